@@ -1,0 +1,308 @@
+"""Benchmark: RK4 system-steps/s of the batched forward on the 2-DOF coupled
+configuration (16384 systems, 200k steps, dt = 1e-3, FP32 with compensated
+state update, checked against the FP64 path).
+
+One "step" of this benchmark is one full solve: every system integrated over
+the whole 200k-step horizon by one persistent kernel launch.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: device-timed (CUDA events on the launching stream) throughput with the
+inputs resident in HBM, L2 flushed (256 MiB write) between timed solves.
+e2e: the same metric through the one-shot C-ABI call pasif_forward with
+pinned host buffers (upload, NVRTC-cached kernel, download) per solve.
+--impl reference: the CPU restatement of the reference's RK4 (FP64, all host
+threads) on a bounded sample of the same workload.
+Multi-GPU: replicas (systems are independent; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK4 system-steps/s (FP32 vs FP64 @<=1e-5 rel err); adjoint grads/s; p99 ms"
+UNIT = "system-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--systems", type=int, default=16384)
+    ap.add_argument("--nsteps", type=int, default=200_000)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count() or 1
+
+
+def cpu_sample_rate(w, seconds: float, threads: int):
+    """FP64 oracle (the reference's RK4 restated, OpenMP over systems) on a
+    bounded sample of the workload: full horizon, a subset of systems."""
+    from oracle import pyoracle as O
+    n_cal = max(threads, 8)
+    t0 = time.perf_counter()
+    O.batch_forward(w.pattern, w.values[:n_cal], w.x0[:n_cal], w.exc_index[:n_cal], w.signals, w.h, w.nsteps,
+                    w.window, w.im, "fp64", threads=threads)
+    dt = time.perf_counter() - t0
+    rate = n_cal * w.nsteps / dt
+    n_s = int(min(w.n_sys, max(n_cal, rate * seconds / w.nsteps)))
+    n_s = max(threads, (n_s // threads) * threads)
+    t0 = time.perf_counter()
+    O.batch_forward(w.pattern, w.values[:n_s], w.x0[:n_s], w.exc_index[:n_s], w.signals, w.h, w.nsteps, w.window,
+                    w.im, "fp64", threads=threads)
+    dt = time.perf_counter() - t0
+    return n_s * w.nsteps / dt, n_s, dt
+
+
+def workload(args):
+    from pasif_gb300 import synth
+    return synth.coupled2(n_sys=args.systems, nsteps=args.nsteps)
+
+
+def config_of(w, args, extra=None):
+    c = {"workload": "coupled_2dof: 16384 systems x 200000 RK4 steps, dt=1e-3, n=5 states "
+                     "(2 DOF + RMS probe), 10 K / 4 quad / 4 cubic / 1 force nnz, 8 band-limited signals, W=8",
+         "systems": w.n_sys, "rk4_steps": w.nsteps, "precision": "fp32_kahan (FP32 stages, compensated update)",
+         "l2": "flushed between timed solves (256 MiB write)", "parallelism": f"replicas x{args.gpus}"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    w = workload(args)
+    threads = host_threads()
+    rates = []
+    sample = None
+    for i in range(args.warmup + args.steps):
+        rate, n_s, dt = cpu_sample_rate(w, args.cpu_seconds / max(1, args.steps), threads)
+        sample = f"{n_s} of {w.n_sys} systems x {w.nsteps} steps (FP64, {dt:.1f} s)"
+        if i >= args.warmup:
+            rates.append(rate)
+    value = float(statistics.median(rates))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * w.n_sys * w.nsteps / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": config_of(w, args, {"precision": "fp64 (reference precision)"}), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+
+    from pasif_gb300 import _native as N
+    from pasif_gb300.batch import Batch, Plan, Signals, forward
+
+    w = workload(args)
+    stream = torch.cuda.Stream()
+    prec = "fp32_kahan"
+    plan = Plan(w.pattern, prec)
+    sig = Signals(w.signals, w.window, w.im, prec, stream=stream)
+    batch = Batch(plan, w.values, w.x0, w.exc_index, stream=stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def solve():
+        batch.forward(sig, w.h, w.nsteps, stream=stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            solve()
+    torch.cuda.synchronize()
+    info = batch.kernel_info()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for e0, e1 in evs:
+                flush.zero_()
+                e0.record(stream)
+                solve()
+                e1.record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+        barrier()
+    kernel_s = sum(e0.elapsed_time(e1) for e0, e1 in evs) * 1e-3
+    t = torch.tensor([kernel_s], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    kernel_s = float(t.item())
+    sys_steps = w.n_sys * w.nsteps
+    value = world * sys_steps * args.steps / kernel_s
+    ms_per_step = 1e3 * kernel_s / args.steps
+    st32, _, _ = batch.get(stream=stream)
+
+    # end to end through the one-shot C-ABI call with pinned host buffers
+    def pinned(a, dtype):
+        t = torch.empty(a.shape, dtype=dtype, pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    hv, hx0 = pinned(w.values, torch.float64), pinned(w.x0, torch.float64)
+    he, hs = pinned(w.exc_index.astype(np.int32), torch.int32), pinned(w.signals, torch.float64)
+    him = pinned(np.asarray(w.im, dtype=np.float64), torch.float64)
+    forward(w.pattern, hv, hx0, he, hs, w.h, w.nsteps, w.window, him, prec)   # warm (NVRTC cache)
+    barrier()
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out, _, _ = forward(w.pattern, hv, hx0, he, hs, w.h, w.nsteps, w.window, him, prec)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_times)
+    tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    e2e_value = world * sys_steps / float(tt.item())
+    h2d = hv.nbytes + hx0.nbytes + he.nbytes + hs.nbytes + him.nbytes
+    d2h = out.nbytes
+
+    # FP64 path on the same workload (one solve) and the FP32 error against it
+    plan64 = Plan(w.pattern, "fp64")
+    sig64 = Signals(w.signals, w.window, w.im, "fp64", stream=stream)
+    b64 = Batch(plan64, w.values, w.x0, w.exc_index, stream=stream)
+    b64.forward(sig64, w.h, w.nsteps, stream=stream)   # warm
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b64.forward(sig64, w.h, w.nsteps, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_value = sys_steps / (e0.elapsed_time(e1) * 1e-3)
+    st64, _, _ = b64.get(stream=stream)
+    T = w.nsteps * w.h
+    rms32, rms64 = np.sqrt(st32[:, 4] / T), np.sqrt(st64[:, 4] / T)
+    rel = np.abs(rms32 - rms64) / np.abs(rms64)
+
+    # roofline: algorithmic FLOPs per launch / launch time vs the measured FMA peak
+    flops_ss = w.pattern.flops_per_step()
+    achieved = flops_ss * sys_steps / (kernel_s / args.steps)
+    import ctypes
+    peak = ctypes.c_double()
+    N.check(N.lib.pasif_fma_peak(N.FP32, ctypes.byref(peak)))
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_coupled2_fp32k.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("dram_bytes_per_launch")
+    clocks = clk.summary()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator pasif_gb300/synth.py)",
+                "config": config_of(w, args), "gpu_launches": args.steps,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "roofline": {"bound": "fp32_fma", "achieved": achieved / 1e12, "peak": peak.value / 1e12,
+                             "unit": "TFLOP/s", "frac": achieved / peak.value, "traffic": traffic,
+                             "peak_source": "measured in this run (pasif_fma_peak: FP32 FMA chains on every SM)",
+                             "flops_per_system_step": flops_ss},
+                "clocks": clocks,
+                "kernel": {"kind": info["kind"], "registers": info["registers"]},
+                "fp64_path": {"value": fp64_value, "unit": UNIT, "speedup_fp32_kahan": value / world / fp64_value},
+                "accuracy": {"max_rel_err_rms_fp32_kahan_vs_fp64": float(rel.max()),
+                             "median_rel_err": float(np.median(rel)), "bound": 1e-5},
+                "wall_s_timed_region": t_wall}
+        if world == 1:
+            rate, n_s, dt = cpu_sample_rate(w, args.cpu_seconds, host_threads())
+            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": host_threads(), "kind": "port",
+                                    "sample": f"{n_s} of {w.n_sys} systems x {w.nsteps} steps, FP64 oracle "
+                                              f"({dt:.1f} s)"}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,194 @@
+"""Native batch interface: many instances of one pattern on the GPU.
+
+    plan = Plan(pattern, "fp32_kahan")
+    sig = Signals(x, window=8, im=weights, precision="fp32_kahan")
+    b = Batch(plan, values, x0, exc_index)        # uploads once
+    b.forward(sig, h, nsteps, sq_comp=[4])         # one persistent kernel
+    state, mx, sq = b.get()
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .system import Pattern, reducers_c
+
+
+def _prec(p) -> int:
+    return N.PRECISIONS[p] if isinstance(p, str) else int(p)
+
+
+def _stream(stream) -> C.c_void_p:
+    if stream is None:
+        return C.c_void_p(0)
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+class Plan:
+    def __init__(self, pattern: Pattern, precision="fp64", generic_only: bool = False):
+        self.pattern = pattern
+        self.precision = _prec(precision)
+        self._c = pattern.to_c()
+        h = C.c_void_p()
+        N.check(N.lib.pasif_plan_create(C.byref(h), C.byref(self._c), self.precision,
+                                        N.PLAN_GENERIC_ONLY if generic_only else 0))
+        self.handle = h
+
+    def jit_report(self, values=None, max_mask: int = 0, sq_mask: int = 0) -> str:
+        """Compiler resource report of the specialised forward kernel (no GPU needed)."""
+        v = N.f64(values) if values is not None else None
+        n_sys = int(v.shape[0]) if v is not None else 0
+        ln = C.c_longlong()
+        N.check(N.lib.pasif_plan_jit_report(self.handle, N.dptr(v) if v is not None else None, n_sys, max_mask,
+                                            sq_mask, None, 0, C.byref(ln)))
+        buf = C.create_string_buffer(ln.value + 1)
+        N.check(N.lib.pasif_plan_jit_report(self.handle, N.dptr(v) if v is not None else None, n_sys, max_mask,
+                                            sq_mask, buf, ln.value + 1, C.byref(ln)))
+        return buf.value.decode()
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            N.lib.pasif_plan_destroy(h)
+            self.handle = None
+
+
+class Signals:
+    """Excitation table (n_exc signals x len samples) in the plan precision.
+    window 0: sample and hold; window W: linear weights im (2W values)."""
+
+    def __init__(self, x, window: int = 0, im=None, precision="fp64", stream=None):
+        x = N.f64(x)
+        if x.ndim == 1:
+            x = x[None, :]
+        self.n_exc, self.len = x.shape
+        self.window = int(window)
+        im_a = N.f64(im).reshape(-1) if im is not None else None
+        h = C.c_void_p()
+        N.check(N.lib.pasif_signals_create(C.byref(h), N.dptr(x), self.n_exc, self.len, self.window,
+                                           N.dptr(im_a) if im_a is not None else None, _prec(precision), N.HOST,
+                                           _stream(stream)))
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            N.lib.pasif_signals_destroy(h)
+            self.handle = None
+
+
+class Batch:
+    """n_sys instances: values[n_sys][P], x0[n_sys][n], exc_index[n_sys].
+    Arrays are numpy (host) or torch CUDA tensors (device, float64, contiguous)."""
+
+    def __init__(self, plan: Plan, values, x0, exc_index, stream=None):
+        self.plan = plan
+        p = plan.pattern
+        self.n_sys = int(len(exc_index))
+        h = C.c_void_p()
+        N.check(N.lib.pasif_batch_create(C.byref(h), plan.handle, self.n_sys))
+        self.handle = h
+        self._h = 0.0
+        self.set(values, x0, exc_index, stream)
+
+    def set(self, values, x0, exc_index, stream=None):
+        p = self.plan.pattern
+        if _is_device(values):
+            mem = N.DEVICE
+            ptrs = [C.c_void_p(t.data_ptr()) for t in (values, x0, exc_index)]
+            self._keep = (values, x0, exc_index)
+        else:
+            mem = N.HOST
+            v = N.f64(values).reshape(self.n_sys, p.P)
+            x = N.f64(x0).reshape(self.n_sys, p.n)
+            e = N.i32(exc_index).reshape(self.n_sys)
+            self._keep = (v, x, e)
+            ptrs = [C.c_void_p(a.ctypes.data) for a in (v, x, e)]
+        N.check(N.lib.pasif_batch_set(self.handle, *ptrs, mem, _stream(stream)))
+
+    def forward(self, signals: Signals, h: float, nsteps: int, step0: int = 0, max_comp=(), max_start: int = 0,
+                sq_comp=(), sq_start: int = 0, stream=None):
+        self._red = reducers_c(max_comp, max_start, sq_comp, sq_start)
+        self._h = float(h)
+        N.check(N.lib.pasif_batch_forward(self.handle, signals.handle, float(h), int(step0), int(nsteps),
+                                          C.byref(self._red), _stream(stream)))
+
+    def get(self, stream=None):
+        """(state[n_sys][n], max[n_sys][n_max], sq[n_sys]) as numpy float64."""
+        p = self.plan.pattern
+        nmax = int(self._red.n_max) if hasattr(self, "_red") else 0
+        st = np.empty((self.n_sys, p.n))
+        mx = np.empty((self.n_sys, max(nmax, 1)))
+        sq = np.empty(self.n_sys)
+        N.check(N.lib.pasif_batch_get(self.handle, C.c_void_p(st.ctypes.data), C.c_void_p(mx.ctypes.data),
+                                      C.c_void_p(sq.ctypes.data), N.HOST, _stream(stream)))
+        return st, mx[:, :nmax], sq
+
+    def get_device(self, state, mx=None, sq=None, stream=None):
+        """Write results into CUDA tensors (float64, contiguous)."""
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+        N.check(N.lib.pasif_batch_get(self.handle, ptr(state), ptr(mx), ptr(sq), N.DEVICE, _stream(stream)))
+
+    def adjoint(self, signals: Signals, h: float, nsteps: int, g_final=None, g_sq=None, sq_comp=(),
+                sq_start: int = 0, stream=None):
+        """Exact discrete adjoint: returns (d_values[n_sys][P], d_x0[n_sys][n])."""
+        p = self.plan.pattern
+        red = reducers_c((), 0, sq_comp, sq_start)
+        gf = N.f64(g_final).reshape(self.n_sys, p.n) if g_final is not None else None
+        gs = N.f64(g_sq).reshape(self.n_sys) if g_sq is not None else None
+        dv = np.empty((self.n_sys, p.P))
+        dx = np.empty((self.n_sys, p.n))
+        vp = lambda a: C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
+        N.check(N.lib.pasif_batch_adjoint(self.handle, signals.handle, float(h), int(nsteps), C.byref(red), vp(gf),
+                                          vp(gs), vp(dv), vp(dx), N.HOST, _stream(stream)))
+        return dv, dx
+
+    def adjoint_device(self, signals: Signals, h: float, nsteps: int, g_final, g_sq, d_values, d_x0, sq_comp=(),
+                       sq_start: int = 0, stream=None):
+        red = reducers_c((), 0, sq_comp, sq_start)
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+        N.check(N.lib.pasif_batch_adjoint(self.handle, signals.handle, float(h), int(nsteps), C.byref(red),
+                                          ptr(g_final), ptr(g_sq), ptr(d_values), ptr(d_x0), N.DEVICE,
+                                          _stream(stream)))
+
+    def kernel_info(self):
+        k, r = C.c_int(), C.c_int()
+        N.check(N.lib.pasif_batch_kernel_info(self.handle, C.byref(k), C.byref(r)))
+        return {"kind": {0: "none", 1: "generic", 2: "specialised"}[k.value], "registers": r.value}
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            N.lib.pasif_batch_destroy(h)
+            self.handle = None
+
+
+def _is_device(a) -> bool:
+    return hasattr(a, "is_cuda") and bool(a.is_cuda)
+
+
+def forward(pattern: Pattern, values, x0, exc_index, x, h: float, nsteps: int, window: int = 0, im=None,
+            precision="fp64", step0: int = 0, max_comp=(), max_start: int = 0, sq_comp=(), sq_start: int = 0):
+    """One-shot forward from host arrays through pasif_forward (upload,
+    integrate, download).  Returns (state, max, sq)."""
+    v = N.f64(values).reshape(-1, pattern.P)
+    n_sys = v.shape[0]
+    x0a = N.f64(x0).reshape(n_sys, pattern.n)
+    e = N.i32(exc_index).reshape(n_sys)
+    xa = N.f64(x)
+    if xa.ndim == 1:
+        xa = xa[None, :]
+    im_a = N.f64(im).reshape(-1) if im is not None else None
+    red = reducers_c(max_comp, max_start, sq_comp, sq_start)
+    c = pattern.to_c()
+    st = np.empty((n_sys, pattern.n))
+    mx = np.empty((n_sys, max(int(red.n_max), 1)))
+    sq = np.empty(n_sys)
+    N.check(N.lib.pasif_forward(C.byref(c), _prec(precision), n_sys, N.dptr(v), N.dptr(x0a), N.iptr(e), N.dptr(xa),
+                                xa.shape[0], xa.shape[1], int(window), N.dptr(im_a) if im_a is not None else None,
+                                float(h), int(step0), int(nsteps), C.byref(red), N.dptr(st), N.dptr(mx), N.dptr(sq)))
+    return st, mx[:, :int(red.n_max)], sq

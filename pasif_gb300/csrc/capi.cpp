@@ -1,0 +1,454 @@
+// capi.cpp -- extern "C" entry points declared in include/pasif_gb300.h.
+#include "../../include/pasif_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "driver.h"
+#include "generic_kernels.h"
+#include "engine.h"
+
+struct pasif_driver {
+    std::unique_ptr<pasif::Driver> d;
+};
+struct pasif_plan {
+    std::shared_ptr<pasif::Plan> p;
+};
+struct pasif_signals {
+    std::shared_ptr<pasif::Signals> s;
+};
+struct pasif_batch {
+    std::unique_ptr<pasif::Batch> b;
+    int n_max = 0;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int done(int rc, const std::string& msg) {
+    if (rc) g_err = msg;
+    return rc;
+}
+
+template <typename F>
+int guard(F&& f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(PASIF_ERR_MEMORY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(PASIF_ERR_INVALID, e.what());
+    }
+}
+
+bool to_pattern(const pasif_pattern* in, pasif::Pattern* out, std::string* err) {
+    if (!in) { *err = "null pattern"; return false; }
+    if (in->n < 0 || in->k_nnz < 0 || in->g_nnz < 0 || in->l_nnz < 0 || in->p_nnz < 0 || in->f_nnz < 0) {
+        *err = "negative pattern size";
+        return false;
+    }
+    if (!in->k_ptr || (in->k_nnz && !in->k_col) || (in->g_nnz && !in->g_idx) || (in->l_nnz && !in->l_idx) ||
+        (in->p_nnz && !in->p_idx) || (in->f_nnz && !in->f_idx)) {
+        *err = "null pattern array";
+        return false;
+    }
+    out->n = in->n;
+    out->n_sp = in->n_sp > 0 ? in->n_sp : in->n;
+    out->k_ptr.assign(in->k_ptr, in->k_ptr + in->n + 1);
+    out->k_col.assign(in->k_col, in->k_col + in->k_nnz);
+    out->g_idx.assign(in->g_idx, in->g_idx + 3LL * in->g_nnz);
+    out->l_idx.assign(in->l_idx, in->l_idx + 4LL * in->l_nnz);
+    out->p_idx.assign(in->p_idx, in->p_idx + 5LL * in->p_nnz);
+    out->f_idx.assign(in->f_idx, in->f_idx + in->f_nnz);
+    *err = out->validate();
+    return err->empty();
+}
+
+bool to_reducers(const pasif_reducers* r, pasif::Reducers* out, std::string* err) {
+    if (!r) return true;
+    if (r->n_max < 0 || r->n_sq < 0 || (r->n_max && !r->max_comp) || (r->n_sq && !r->sq_comp)) {
+        *err = "bad reducer description";
+        return false;
+    }
+    out->max_comp.assign(r->max_comp, r->max_comp + r->n_max);
+    out->max_start = r->max_start;
+    out->sq_comp.assign(r->sq_comp, r->sq_comp + r->n_sq);
+    out->sq_start = r->sq_start;
+    return true;
+}
+
+int copy_out(const std::vector<double>& v, double* out, long long cap, long long* out_len) {
+    if (out_len) *out_len = (long long)v.size();
+    if (!out) return PASIF_OK;
+    if (cap < (long long)v.size()) return fail(PASIF_ERR_INVALID, "output capacity too small");
+    std::copy(v.begin(), v.end(), out);
+    return PASIF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pasif_last_error(void) { return g_err.c_str(); }
+
+int pasif_version(void) { return 100; }
+
+int pasif_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+/* ---------------- drop-in driver ---------------- */
+
+int pasif_driver_create(pasif_driver** out, const double* const* signals, const long long* lengths, int n_signals,
+                        unsigned sample_rate, unsigned numsteps, int d_compute, int d_system, int d_solver,
+                        unsigned gpu_id) {
+    return guard([&] {
+        if (!out) return fail(PASIF_ERR_INVALID, "null output handle");
+        if (n_signals > 0 && (!signals || !lengths)) return fail(PASIF_ERR_INVALID, "null signal arrays");
+        std::unique_ptr<pasif_driver> h(new pasif_driver());
+        h->d.reset(new pasif::Driver(gpu_id, sample_rate, numsteps, d_compute != 0, d_system != 0, d_solver != 0));
+        std::string err;
+        int rc = h->d->load_excitations(signals, lengths, n_signals, sample_rate, &err);
+        if (rc && rc != PASIF_ERR_LENGTH && rc != PASIF_ERR_INVALID) return fail(rc, err);
+        *out = h.release();
+        return PASIF_OK;
+    });
+}
+
+int pasif_driver_destroy(pasif_driver* d) {
+    delete d;
+    return PASIF_OK;
+}
+
+#define DRV_CHECK(d) \
+    if (!(d) || !(d)->d) return fail(PASIF_ERR_INVALID, "null driver");
+
+int pasif_driver_set_precision(pasif_driver* d, int precision) {
+    DRV_CHECK(d);
+    std::string err;
+    return done(d->d->set_precision(precision, &err), err);
+}
+
+int pasif_driver_set_fwd_k(pasif_driver* d, unsigned rows, unsigned cols, const double* values,
+                           const unsigned* indices, const unsigned* indptr, long long nnz) {
+    DRV_CHECK(d);
+    return guard([&] {
+        std::string err;
+        return done(d->d->set_k(true, rows, cols, values, indices, indptr, nnz, &err), err);
+    });
+}
+
+int pasif_driver_set_bwd_k(pasif_driver* d, unsigned rows, unsigned cols, const double* values,
+                           const unsigned* indices, const unsigned* indptr, long long nnz) {
+    DRV_CHECK(d);
+    return guard([&] {
+        std::string err;
+        return done(d->d->set_k(false, rows, cols, values, indices, indptr, nnz, &err), err);
+    });
+}
+
+#define DRV_COO(name, fwd, order)                                                                   \
+    int name(pasif_driver* d, const unsigned dims[order], const double* values, const unsigned* indices, \
+             long long nnz) {                                                                       \
+        DRV_CHECK(d);                                                                               \
+        return guard([&] {                                                                          \
+            std::string err;                                                                        \
+            return done(d->d->set_coo(fwd, order, dims, values, indices, nnz, &err), err);          \
+        });                                                                                         \
+    }
+
+DRV_COO(pasif_driver_set_fwd_gamma, true, 3)
+DRV_COO(pasif_driver_set_bwd_gamma, false, 3)
+DRV_COO(pasif_driver_set_fwd_lambda, true, 4)
+DRV_COO(pasif_driver_set_bwd_lambda, false, 4)
+DRV_COO(pasif_driver_set_fwd_psi, true, 5)
+DRV_COO(pasif_driver_set_bwd_psi, false, 5)
+
+int pasif_driver_set_fwd_force_pattern(pasif_driver* d, const double* pattern, long long n) {
+    DRV_CHECK(d);
+    return guard([&] { std::string err; return done(d->d->set_force(true, pattern, n, &err), err); });
+}
+
+int pasif_driver_set_bwd_force_pattern(pasif_driver* d, const double* pattern, long long n) {
+    DRV_CHECK(d);
+    return guard([&] { std::string err; return done(d->d->set_force(false, pattern, n, &err), err); });
+}
+
+int pasif_driver_set_fwd_initial_conditions(pasif_driver* d, const double* ic, long long n) {
+    DRV_CHECK(d);
+    return guard([&] { std::string err; return done(d->d->set_ic(true, ic, n, &err), err); });
+}
+
+int pasif_driver_set_bwd_initial_conditions(pasif_driver* d, const double* ic, long long n) {
+    DRV_CHECK(d);
+    return guard([&] { std::string err; return done(d->d->set_ic(false, ic, n, &err), err); });
+}
+
+int pasif_driver_allocate_system(pasif_driver* d) {
+    DRV_CHECK(d);
+    return guard([&] { std::string err; return done(d->d->allocate_system(&err), err); });
+}
+
+int pasif_driver_allocate_adjoint(pasif_driver* d) {
+    DRV_CHECK(d);
+    return guard([&] { std::string err; return done(d->d->allocate_adjoint(&err), err); });
+}
+
+int pasif_driver_load_excitations(pasif_driver* d, const double* const* signals, const long long* lengths,
+                                  int n_signals, unsigned sample_rate) {
+    DRV_CHECK(d);
+    return guard([&] {
+        if (n_signals > 0 && (!signals || !lengths)) return fail(PASIF_ERR_INVALID, "null signal arrays");
+        std::string err;
+        return done(d->d->load_excitations(signals, lengths, n_signals, sample_rate, &err), err);
+    });
+}
+
+int pasif_driver_set_interpolation_matrix(pasif_driver* d, const double* matrix, long long size, unsigned window) {
+    DRV_CHECK(d);
+    return guard([&] { std::string err; return done(d->d->set_interp(matrix, size, window, &err), err); });
+}
+
+int pasif_driver_set_modulation_buffer(pasif_driver* d, const double* buffer, long long n) {
+    DRV_CHECK(d);
+    return guard([&] { std::string err; return done(d->d->set_modulation(buffer, n, &err), err); });
+}
+
+int pasif_driver_get_amplitudes(pasif_driver* d, double* out, long long capacity, long long* out_len) {
+    DRV_CHECK(d);
+    return guard([&] {
+        std::vector<double> v;
+        std::string err;
+        int rc = d->d->amplitudes(&v, &err);
+        if (rc) return fail(rc, err);
+        return copy_out(v, out, capacity, out_len);
+    });
+}
+
+int pasif_driver_get_trajectory(pasif_driver* d, unsigned save_steps, double* out, long long capacity,
+                                long long* out_len) {
+    DRV_CHECK(d);
+    return guard([&] {
+        std::vector<double> v;
+        std::string err;
+        int rc = d->d->trajectory(save_steps, &v, &err);
+        if (rc) return fail(rc, err);
+        return copy_out(v, out, capacity, out_len);
+    });
+}
+
+int pasif_driver_get_gradient(pasif_driver* d, unsigned save, double* out, long long capacity, long long* out_len) {
+    DRV_CHECK(d);
+    return guard([&] {
+        std::vector<double> v;
+        std::string err;
+        int rc = d->d->gradient(save, &v, &err);
+        if (rc) return fail(rc, err);
+        return copy_out(v, out, capacity, out_len);
+    });
+}
+
+int pasif_driver_last_kernel(pasif_driver* d, int* kind) {
+    DRV_CHECK(d);
+    if (!kind) return fail(PASIF_ERR_INVALID, "null output");
+    *kind = d->d->last_kind();
+    return PASIF_OK;
+}
+
+/* ---------------- native batches ---------------- */
+
+int pasif_plan_create(pasif_plan** out, const pasif_pattern* pattern, int precision, int flags) {
+    return guard([&] {
+        if (!out) return fail(PASIF_ERR_INVALID, "null output handle");
+        pasif::Pattern pat;
+        std::string err;
+        if (!to_pattern(pattern, &pat, &err)) return fail(PASIF_ERR_INVALID, err);
+        std::unique_ptr<pasif_plan> h(new pasif_plan());
+        int rc = pasif::plan_create(pat, precision, (flags & PASIF_PLAN_GENERIC_ONLY) != 0, &h->p, &err);
+        if (rc) return fail(rc, err);
+        *out = h.release();
+        return PASIF_OK;
+    });
+}
+
+int pasif_plan_destroy(pasif_plan* p) {
+    delete p;
+    return PASIF_OK;
+}
+
+int pasif_signals_create(pasif_signals** out, const double* x, int n_exc, int len, int window, const double* im,
+                         int precision, int memory, void* stream) {
+    return guard([&] {
+        if (!out) return fail(PASIF_ERR_INVALID, "null output handle");
+        std::unique_ptr<pasif_signals> h(new pasif_signals());
+        std::string err;
+        int rc = pasif::signals_create(x, n_exc, len, window, im, precision, memory, (cudaStream_t)stream, &h->s, &err);
+        if (rc) return fail(rc, err);
+        *out = h.release();
+        return PASIF_OK;
+    });
+}
+
+int pasif_signals_destroy(pasif_signals* s) {
+    delete s;
+    return PASIF_OK;
+}
+
+int pasif_batch_create(pasif_batch** out, pasif_plan* plan, int n_sys) {
+    return guard([&] {
+        if (!out || !plan) return fail(PASIF_ERR_INVALID, "null handle");
+        std::unique_ptr<pasif_batch> h(new pasif_batch());
+        std::string err;
+        int rc = pasif::batch_create(plan->p, n_sys, &h->b, &err);
+        if (rc) return fail(rc, err);
+        *out = h.release();
+        return PASIF_OK;
+    });
+}
+
+int pasif_batch_destroy(pasif_batch* b) {
+    delete b;
+    return PASIF_OK;
+}
+
+int pasif_batch_set(pasif_batch* b, const double* values, const double* x0, const int* exc_index, int memory,
+                    void* stream) {
+    if (!b || !b->b) return fail(PASIF_ERR_INVALID, "null batch");
+    return guard([&] {
+        std::string err;
+        return done(b->b->set(values, x0, exc_index, memory, (cudaStream_t)stream, &err), err);
+    });
+}
+
+int pasif_batch_forward(pasif_batch* b, const pasif_signals* s, double h, int step0, int nsteps,
+                        const pasif_reducers* red, void* stream) {
+    if (!b || !b->b || !s || !s->s) return fail(PASIF_ERR_INVALID, "null handle");
+    return guard([&] {
+        pasif::Reducers r;
+        std::string err;
+        if (!to_reducers(red, &r, &err)) return fail(PASIF_ERR_INVALID, err);
+        return done(b->b->forward(*s->s, h, step0, nsteps, r, 0, 0, (cudaStream_t)stream, &err), err);
+    });
+}
+
+int pasif_batch_get(pasif_batch* b, double* state, double* max, double* sq, int memory, void* stream) {
+    if (!b || !b->b) return fail(PASIF_ERR_INVALID, "null batch");
+    return guard([&] {
+        std::string err;
+        return done(b->b->get(state, max, sq, b->b->last_h, memory, (cudaStream_t)stream, &err), err);
+    });
+}
+
+int pasif_batch_adjoint(pasif_batch* b, const pasif_signals* s, double h, int nsteps, const pasif_reducers* red,
+                        const double* g_final, const double* g_sq, double* d_values, double* d_x0, int memory,
+                        void* stream) {
+    if (!b || !b->b || !s || !s->s) return fail(PASIF_ERR_INVALID, "null handle");
+    return guard([&] {
+        pasif::Reducers r;
+        std::string err;
+        if (!to_reducers(red, &r, &err)) return fail(PASIF_ERR_INVALID, err);
+        return done(b->b->adjoint(*s->s, h, nsteps, r, g_final, g_sq, d_values, d_x0, memory, (cudaStream_t)stream,
+                                  &err),
+                    err);
+    });
+}
+
+int pasif_batch_kernel_info(pasif_batch* b, int* kind, int* registers) {
+    if (!b || !b->b) return fail(PASIF_ERR_INVALID, "null batch");
+    if (kind) *kind = b->b->last_kind;
+    if (registers) *registers = b->b->last_kind == pasif::kSpecialised ? b->b->last_jit.regs : 0;
+    return PASIF_OK;
+}
+
+int pasif_fma_peak(int precision, double* flops_per_second) {
+    if (!flops_per_second) return fail(PASIF_ERR_INVALID, "null output");
+    cudaError_t e = pk::measure_fma_peak(precision != PASIF_FP64, flops_per_second);
+    if (e != cudaSuccess) return fail(PASIF_ERR_CUDA, pasif::cuda_err("FMA peak probe", e));
+    return PASIF_OK;
+}
+
+int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys, unsigned long long max_mask,
+                          unsigned long long sq_mask, char* log, long long capacity, long long* out_len) {
+    if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null plan");
+    return guard([&] {
+        const pasif::Pattern& pat = p->p->pat;
+        const int P = pat.P();
+        const bool f32 = p->p->precision != pasif::kFP64;
+        pasif::Literals lit;
+        lit.is_lit.assign(P, 0);
+        lit.value.assign(P, 0.0);
+        if (values && n_sys > 0)
+            for (int q = 0; q < P; ++q) {
+                bool same = true;
+                const double v0 = f32 ? (double)(float)values[q] : values[q];
+                for (int b = 1; b < n_sys && same; ++b) {
+                    const double v = f32 ? (double)(float)values[(long long)b * P + q] : values[(long long)b * P + q];
+                    same = v == v0 && std::signbit(v) == std::signbit(v0);
+                }
+                lit.is_lit[q] = same && std::isfinite(v0);
+                lit.value[q] = v0;
+            }
+        pasif::FwdKernelKey key;
+        key.f32 = f32;
+        key.kahan = p->p->precision == pasif::kFP32Kahan;
+        key.max_mask = max_mask;
+        key.sq_mask = sq_mask;
+        std::string report, err;
+        if (!pasif::fwd_compile_report(pat, lit, key, &report, &err)) return fail(PASIF_ERR_NVRTC, err);
+        if (out_len) *out_len = (long long)report.size();
+        if (log && capacity > 0) {
+            const size_t n = std::min<size_t>(report.size(), (size_t)capacity - 1);
+            std::memcpy(log, report.data(), n);
+            log[n] = '\0';
+        }
+        return PASIF_OK;
+    });
+}
+
+int pasif_forward(const pasif_pattern* pattern, int precision, int n_sys, const double* values, const double* x0,
+                  const int* exc_index, const double* x, int n_exc, int len, int window, const double* im, double h,
+                  int step0, int nsteps, const pasif_reducers* red, double* state, double* max, double* sq) {
+    return guard([&] {
+        pasif::Pattern pat;
+        std::string err;
+        if (!to_pattern(pattern, &pat, &err)) return fail(PASIF_ERR_INVALID, err);
+        pasif::Reducers r;
+        if (!to_reducers(red, &r, &err)) return fail(PASIF_ERR_INVALID, err);
+        std::shared_ptr<pasif::Plan> plan;
+        int rc = pasif::plan_create(pat, precision, false, &plan, &err);
+        if (rc) return fail(rc, err);
+        std::shared_ptr<pasif::Signals> sig;
+        rc = pasif::signals_create(x, n_exc, len, window, im, precision, pasif::kHost, 0, &sig, &err);
+        if (rc) return fail(rc, err);
+        std::unique_ptr<pasif::Batch> bt;
+        rc = pasif::batch_create(plan, n_sys, &bt, &err);
+        if (rc) return fail(rc, err);
+        rc = bt->set(values, x0, exc_index, pasif::kHost, 0, &err);
+        if (rc) return fail(rc, err);
+        rc = bt->forward(*sig, h, step0, nsteps, r, 0, 0, 0, &err);
+        if (rc) return fail(rc, err);
+        rc = bt->get(state, max, sq, h, pasif::kHost, 0, &err);
+        if (rc) return fail(rc, err);
+        return PASIF_OK;
+    });
+}
+
+}  // extern "C"

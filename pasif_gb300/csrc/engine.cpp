@@ -1,0 +1,515 @@
+// engine.cpp -- host side of the batched RK4 engine (plans, signal tables,
+// device-resident batches, kernel selection and launch).
+#include "engine.h"
+
+#include <cmath>
+#include <cstring>
+
+#include "generic_kernels.h"
+
+namespace pasif {
+
+std::string cuda_err(const char* what, cudaError_t e) {
+    return std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+}
+
+#define PK_CUDA(call, what)                          \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) {                     \
+            *err = cuda_err(what, e_);               \
+            return e_ == cudaErrorMemoryAllocation ? 4 : 2; \
+        }                                            \
+    } while (0)
+
+DevBuf::~DevBuf() { release(); }
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+cudaError_t DevBuf::ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    else p = nullptr;
+    return e;
+}
+
+static bool is_pow2(unsigned w) { return w && !(w & (w - 1)); }
+
+static cudaMemcpyKind kind_in(int memory) { return memory == kDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice; }
+
+// Copy a double array (host or device) into a device buffer converted to the
+// compute precision.
+static int upload_conv(const double* src, long long n, bool f32, int memory, DevBuf& dst, DevBuf& stage,
+                       cudaStream_t st, std::string* err) {
+    const size_t rs = f32 ? sizeof(float) : sizeof(double);
+    PK_CUDA(dst.ensure((size_t)(n > 0 ? n : 1) * rs), "cudaMalloc");
+    if (n == 0) return 0;
+    if (!f32) {
+        PK_CUDA(cudaMemcpyAsync(dst.p, src, (size_t)n * sizeof(double), kind_in(memory), st), "cudaMemcpyAsync");
+        return 0;
+    }
+    const double* dsrc = src;
+    if (memory == kHost) {
+        PK_CUDA(stage.ensure((size_t)n * sizeof(double)), "cudaMalloc");
+        PK_CUDA(cudaMemcpyAsync(stage.p, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st),
+                "cudaMemcpyAsync");
+        dsrc = stage.as<double>();
+    }
+    PK_CUDA(pk::launch_convert(dsrc, dst.p, n, true, st), "convert kernel");
+    return 0;
+}
+
+// [B][k] double (host or device) -> [k][B] compute precision.
+static int upload_interleaved(const double* src, int B, int k, bool f32, int memory, DevBuf& dst,
+                              DevBuf& stage, cudaStream_t st, std::string* err) {
+    const size_t rs = f32 ? sizeof(float) : sizeof(double);
+    const long long total = (long long)B * k;
+    PK_CUDA(dst.ensure((size_t)(total > 0 ? total : 1) * rs), "cudaMalloc");
+    if (total == 0) return 0;
+    const double* dsrc = src;
+    if (memory == kHost) {
+        PK_CUDA(stage.ensure((size_t)total * sizeof(double)), "cudaMalloc");
+        PK_CUDA(cudaMemcpyAsync(stage.p, src, (size_t)total * sizeof(double), cudaMemcpyHostToDevice, st),
+                "cudaMemcpyAsync");
+        dsrc = stage.as<double>();
+    }
+    PK_CUDA(pk::launch_to_interleaved(dsrc, dst.p, B, k, f32, st), "layout kernel");
+    return 0;
+}
+
+// [k][B] (compute precision or double) -> [B][k] double (host or device).
+static int download_interleaved(const void* src, int B, int k, bool f32, double scale, double* out, int memory,
+                                DevBuf& stage, cudaStream_t st, std::string* err) {
+    const long long total = (long long)B * k;
+    if (total == 0 || !out) return 0;
+    double* ddst = out;
+    if (memory == kHost) {
+        PK_CUDA(stage.ensure((size_t)total * sizeof(double)), "cudaMalloc");
+        ddst = stage.as<double>();
+    }
+    PK_CUDA(pk::launch_from_interleaved(src, ddst, B, k, f32, st, scale), "layout kernel");
+    if (memory == kHost) {
+        PK_CUDA(cudaMemcpyAsync(out, ddst, (size_t)total * sizeof(double), cudaMemcpyDeviceToHost, st),
+                "cudaMemcpyAsync");
+        PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    }
+    return 0;
+}
+
+int signals_create(const double* x, int n_exc, int len, int window, const double* im, int precision,
+                   int memory, cudaStream_t st, std::shared_ptr<Signals>* out, std::string* err) {
+    if (n_exc < 1 || len < 1 || !x) { *err = "excitation table must hold at least one sample of one signal"; return 1; }
+    if (window < 0 || (window > 0 && !is_pow2((unsigned)window))) {
+        *err = "interpolation window size must be a power of two (src/kernels.cu:115-117 masks with W-1)";
+        return 1;
+    }
+    if (window > 0 && !im) { *err = "interpolation matrix missing"; return 1; }
+    auto s = std::make_shared<Signals>();
+    s->f32 = precision != kFP64;
+    s->n_exc = n_exc;
+    s->len = len;
+    s->w = (unsigned)window;
+    s->lw = 0;
+    while (window > 0 && (1u << s->lw) < s->w) s->lw++;
+    DevBuf stage;
+    int rc = upload_conv(x, (long long)n_exc * len, s->f32, memory, s->x, stage, st, err);
+    if (rc) return rc;
+    if (window > 0) {
+        rc = upload_conv(im, 2LL * window, s->f32, memory, s->im, stage, st, err);
+        if (rc) return rc;
+    }
+    PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    *out = s;
+    return 0;
+}
+
+pk::GenPattern Plan::gen() const {
+    pk::GenPattern g;
+    g.data = gpat.as<int>();
+    g.n = pat.n;
+    g.n_sp = pat.n_sp;
+    g.k_nnz = pat.k_nnz();
+    g.g_nnz = pat.g_nnz();
+    g.l_nnz = pat.l_nnz();
+    g.p_nnz = pat.p_nnz();
+    g.f_nnz = pat.f_nnz();
+    g.P = pat.P();
+    return g;
+}
+
+int plan_create(const Pattern& pat, int precision, bool generic_only, std::shared_ptr<Plan>* out,
+                std::string* err) {
+    std::string v = pat.validate();
+    if (!v.empty()) { *err = v; return 1; }
+    if (precision < kFP64 || precision > kFP32Kahan) { *err = "unknown precision"; return 1; }
+    auto p = std::make_shared<Plan>();
+    p->pat = pat;
+    p->precision = precision;
+    p->generic_only = generic_only;
+    *out = p;
+    return 0;
+}
+
+int Plan::ensure_device(std::string* err) {
+    if (gpat.p) return 0;
+    std::vector<int> flat = pat.flat();
+    PK_CUDA(gpat.ensure(flat.size() * sizeof(int)), "cudaMalloc");
+    PK_CUDA(cudaMemcpy(gpat.p, flat.data(), flat.size() * sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
+    return 0;
+}
+
+int batch_create(std::shared_ptr<Plan> plan, int B, std::unique_ptr<Batch>* out, std::string* err) {
+    if (!plan) { *err = "null plan"; return 1; }
+    if (B < 0) { *err = "negative number of systems"; return 1; }
+    std::unique_ptr<Batch> b(new Batch());
+    b->plan = plan;
+    b->B = B;
+    *out = std::move(b);
+    return 0;
+}
+
+int Batch::set(const double* values, const double* x0h, const int* exc_index, int memory, cudaStream_t st,
+               std::string* err) {
+    const Pattern& pat = plan->pat;
+    const int P = pat.P(), n = pat.n;
+    const bool f = f32();
+    if (B > 0 && ((P > 0 && !values) || !x0h || !exc_index)) { *err = "null input array"; return 1; }
+    if (int rc0 = plan->ensure_device(err)) return rc0;
+    int rc = upload_interleaved(values, B, P, f, memory, vals, stage, st, err);
+    if (rc) return rc;
+    rc = upload_interleaved(x0h, B, n, f, memory, x0, stage, st, err);
+    if (rc) return rc;
+    PK_CUDA(exc.ensure((size_t)(B > 0 ? B : 1) * sizeof(int)), "cudaMalloc");
+    std::vector<int> idx(B);
+    if (B > 0) {
+        if (memory == kHost) std::memcpy(idx.data(), exc_index, sizeof(int) * B);
+        else PK_CUDA(cudaMemcpy(idx.data(), exc_index, sizeof(int) * B, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        PK_CUDA(cudaMemcpyAsync(exc.p, idx.data(), sizeof(int) * B, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    }
+    max_exc_ = -1;
+    for (int i = 0; i < B; ++i) {
+        if (idx[i] < 0) { *err = "negative excitation index"; return 1; }
+        if (idx[i] > max_exc_) max_exc_ = idx[i];
+    }
+    // values shared by every instance become compile-time constants
+    lit.is_lit.assign(P, 0);
+    lit.value.assign(P, 0.0);
+    if (memory == kHost && B > 0) {
+        for (int q = 0; q < P; ++q) {
+            bool same = true;
+            if (f) {
+                const float v0 = (float)values[q];
+                for (int b = 1; b < B && same; ++b) {
+                    const float v = (float)values[(long long)b * P + q];
+                    same = std::memcmp(&v, &v0, sizeof(float)) == 0;
+                }
+                lit.value[q] = (double)v0;
+            } else {
+                const double v0 = values[q];
+                for (int b = 1; b < B && same; ++b)
+                    same = std::memcmp(&values[(long long)b * P + q], &v0, sizeof(double)) == 0;
+                lit.value[q] = v0;
+            }
+            lit.is_lit[q] = same && std::isfinite(lit.value[q]) ? 1 : 0;
+        }
+    }
+    PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    return 0;
+}
+
+static int check_comps(const std::vector<int>& c, int n, const char* what, unsigned long long* mask, std::string* err) {
+    *mask = 0;
+    int prev = -1;
+    for (int v : c) {
+        if (v < 0 || v >= n || v >= 64 || v <= prev) {
+            *err = std::string(what) + " components must be ascending, unique, < n and < 64";
+            return 1;
+        }
+        *mask |= 1ull << v;
+        prev = v;
+    }
+    return 0;
+}
+
+template <typename R>
+static void fill_fwd(pk::FwdArgs<R>& a, Batch& bt, const Signals& sig, double h, int step0, int nsteps,
+                     const Reducers& red, unsigned long long mm, unsigned long long sm, int traj_every,
+                     long long traj_slots) {
+    std::memset(&a, 0, sizeof(a));
+    a.vals = bt.vals.as<R>();
+    a.state = bt.state.as<R>();
+    a.exc_index = bt.exc.as<int>();
+    a.scratch = bt.scratch.as<R>();
+    a.out_max = bt.out_max.as<R>();
+    a.out_sq = bt.out_sq.as<R>();
+    a.traj = traj_every > 0 ? bt.traj.as<R>() : nullptr;
+    a.traj_slots = traj_slots;
+    a.traj_every = traj_every > 0 ? traj_every : 1;
+    a.frc = sig.forcing<R>();
+    a.gp = bt.plan->gen();
+    a.h = (R)h;
+    a.h2 = (R)(h / 2.0);
+    a.h6 = (R)(h / 6.0);
+    a.B = bt.B;
+    a.step0 = (unsigned)step0;
+    a.nsteps = nsteps;
+    a.max_start = red.max_start;
+    a.sq_start = red.sq_start;
+    a.max_mask = mm;
+    a.sq_mask = sm;
+}
+
+int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Reducers& red, int traj_every,
+                   long long traj_slots, cudaStream_t st, std::string* err) {
+    const Pattern& pat = plan->pat;
+    const int n = pat.n;
+    const bool f = f32();
+    if (sig.f32 != f) { *err = "signal table precision differs from the plan's"; return 1; }
+    if (step0 < 0 || nsteps < 0) { *err = "negative step index or step count"; return 1; }
+    if (max_exc_ >= sig.n_exc) { *err = "excitation index beyond the signal table"; return 1; }
+    if (!(h > 0.0) || !std::isfinite(h)) { *err = "time step must be positive and finite"; return 1; }
+    unsigned long long mm = 0, sm = 0;
+    if (check_comps(red.max_comp, n, "max reducer", &mm, err)) return 1;
+    if (check_comps(red.sq_comp, n, "sum-of-squares reducer", &sm, err)) return 1;
+    n_max = (int)red.max_comp.size();
+    has_sq = !red.sq_comp.empty();
+    last_h = h;
+    const size_t rs = rsize();
+    const size_t Bn = (size_t)(B > 0 ? B : 1);
+    PK_CUDA(state.ensure(Bn * (size_t)n * rs), "cudaMalloc");
+    PK_CUDA(out_max.ensure(Bn * (size_t)(n_max > 0 ? n_max : 1) * rs), "cudaMalloc");
+    PK_CUDA(out_sq.ensure(Bn * rs), "cudaMalloc");
+    if (traj_every > 0) PK_CUDA(traj.ensure(Bn * (size_t)n * (size_t)(traj_slots > 0 ? traj_slots : 1) * rs), "cudaMalloc");
+    if (B == 0) { last_kind = kNone; return 0; }
+    PK_CUDA(cudaMemcpyAsync(state.p, x0.p, (size_t)B * n * rs, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
+    const bool kahan = plan->precision == kFP32Kahan;
+    if (!plan->generic_only && n <= kJitMaxN) {
+        FwdKernelKey key;
+        key.f32 = f;
+        key.kahan = kahan;
+        key.max_mask = mm;
+        key.sq_mask = sm;
+        key.traj = traj_every > 0;
+        key.block = 128;
+        JitKernel k;
+        std::string jerr;
+        if (get_fwd_kernel(pat, lit, key, &k, &jerr)) {
+            dim3 grid((unsigned)((B + k.block - 1) / k.block));
+            cudaError_t e;
+            if (f) {
+                pk::FwdArgs<float> a;
+                fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
+                void* args[] = {&a};
+                e = cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, 0, st);
+            } else {
+                pk::FwdArgs<double> a;
+                fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
+                void* args[] = {&a};
+                e = cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, 0, st);
+            }
+            PK_CUDA(e, "specialised forward kernel launch");
+            last_kind = kSpecialised;
+            last_jit = k;
+            return 0;
+        }
+        last_jit_error = jerr;
+    }
+    PK_CUDA(scratch.ensure(Bn * 6 * (size_t)n * rs), "cudaMalloc");
+    cudaError_t e;
+    if (f) {
+        pk::FwdArgs<float> a;
+        fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
+        e = pk::launch_gen_fwd(a, kahan, st);
+    } else {
+        pk::FwdArgs<double> a;
+        fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
+        e = pk::launch_gen_fwd(a, kahan, st);
+    }
+    PK_CUDA(e, "generic forward kernel launch");
+    last_kind = kGeneric;
+    return 0;
+}
+
+int Batch::get(double* state_out, double* max_out, double* sq_out, double h, int memory, cudaStream_t st,
+               std::string* err) {
+    const int n = plan->pat.n;
+    const bool f = f32();
+    int rc = download_interleaved(state.p, B, n, f, 1.0, state_out, memory, stage, st, err);
+    if (rc) return rc;
+    if (max_out && n_max > 0) {
+        rc = download_interleaved(out_max.p, B, n_max, f, 1.0, max_out, memory, stage, st, err);
+        if (rc) return rc;
+    }
+    if (sq_out && has_sq) {
+        rc = download_interleaved(out_sq.p, B, 1, f, h, sq_out, memory, stage, st, err);
+        if (rc) return rc;
+    }
+    PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    return 0;
+}
+
+int Batch::get_traj(double* out, long long slots, int memory, cudaStream_t st, std::string* err) {
+    // [slots][n][B] -> [slots][B][n]
+    const int n = plan->pat.n;
+    const bool f = f32();
+    const size_t rs = rsize();
+    for (long long s = 0; s < slots; ++s) {
+        const char* src = traj.as<char>() + (size_t)s * n * B * rs;
+        int rc = download_interleaved(src, B, n, f, 1.0, out + (size_t)s * n * B, memory, stage, st, err);
+        if (rc) return rc;
+    }
+    PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    return 0;
+}
+
+int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red, const double* g_final,
+                   const double* g_sq, double* d_values, double* d_x0, int memory, cudaStream_t st,
+                   std::string* err) {
+    const Pattern& pat = plan->pat;
+    const int n = pat.n, P = pat.P();
+    const bool f = f32();
+    if (sig.f32 != f) { *err = "signal table precision differs from the plan's"; return 1; }
+    if (nsteps < 0) { *err = "negative step count"; return 1; }
+    if (max_exc_ >= sig.n_exc) { *err = "excitation index beyond the signal table"; return 1; }
+    if (!(h > 0.0) || !std::isfinite(h)) { *err = "time step must be positive and finite"; return 1; }
+    unsigned long long sm = 0;
+    if (check_comps(red.sq_comp, n, "sum-of-squares reducer", &sm, err)) return 1;
+    if (B == 0) return 0;
+    const int C = nsteps > 0 ? (int)std::ceil(std::sqrt((double)nsteps)) : 1;
+    const int nck = nsteps > 0 ? (nsteps + C - 1) / C : 0;
+    const size_t rs = rsize();
+    const size_t Bn = (size_t)B;
+    PK_CUDA(ckpt.ensure(Bn * 2 * n * (size_t)(nck > 0 ? nck : 1) * rs), "cudaMalloc");
+    PK_CUDA(buf.ensure(Bn * (size_t)n * (size_t)C * rs), "cudaMalloc");
+    PK_CUDA(scratch.ensure(Bn * 13 * (size_t)n * rs), "cudaMalloc");
+    PK_CUDA(pbar.ensure(Bn * (size_t)(P > 0 ? P : 1) * sizeof(double)), "cudaMalloc");
+    PK_CUDA(dx0.ensure(Bn * (size_t)n * rs), "cudaMalloc");
+    if (g_final) {
+        int rc = upload_interleaved(g_final, B, n, f, memory, gfin, adj_stage, st, err);
+        if (rc) return rc;
+    }
+    if (g_sq) {
+        int rc = upload_conv(g_sq, B, f, memory, gsq, adj_stage, st, err);
+        if (rc) return rc;
+    }
+    cudaError_t e;
+#define PK_FILL_ADJ(R_)                                               \
+    pk::AdjArgs<R_> a;                                                \
+    std::memset(&a, 0, sizeof(a));                                    \
+    a.vals = vals.as<R_>();                                           \
+    a.x0 = x0.as<R_>();                                               \
+    a.exc_index = exc.as<int>();                                      \
+    a.ckpt = ckpt.as<R_>();                                           \
+    a.buf = buf.as<R_>();                                             \
+    a.scratch = scratch.as<R_>();                                     \
+    a.pbar = pbar.as<double>();                                       \
+    a.dx0 = dx0.as<R_>();                                             \
+    a.g_final = g_final ? gfin.as<R_>() : nullptr;                    \
+    a.g_sq = g_sq ? gsq.as<R_>() : nullptr;                           \
+    a.frc = sig.forcing<R_>();                                        \
+    a.gp = plan->gen();                                               \
+    a.h = (R_)h;                                                      \
+    a.h2 = (R_)(h / 2.0);                                             \
+    a.h6 = (R_)(h / 6.0);                                             \
+    a.B = B;                                                          \
+    a.nsteps = nsteps;                                                \
+    a.C = C;                                                          \
+    a.nck = nck;                                                      \
+    a.kahan = plan->precision == kFP32Kahan ? 1 : 0;                  \
+    a.sq_start = red.sq_start;                                        \
+    a.sq_mask = g_sq ? sm : 0ull;
+    if (f) {
+        PK_FILL_ADJ(float)
+        e = pk::launch_gen_adj(a, st);
+    } else {
+        PK_FILL_ADJ(double)
+        e = pk::launch_gen_adj(a, st);
+    }
+#undef PK_FILL_ADJ
+    PK_CUDA(e, "adjoint kernel launch");
+    int rc = download_interleaved(pbar.p, B, P, false, 1.0, d_values, memory, adj_stage, st, err);
+    if (rc) return rc;
+    rc = download_interleaved(dx0.p, B, n, f, 1.0, d_x0, memory, adj_stage, st, err);
+    if (rc) return rc;
+    PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    return 0;
+}
+
+int refgrad_run(const Plan& fwd, const Plan& bwd, int B, const double* fvals, const double* bvals,
+                const double* x0h, const double* a0h, const int* exc_index, const Signals& sig, double h,
+                int nsteps, int save, double* out, cudaStream_t st, std::string* err) {
+    const int nf = fwd.pat.n, na = bwd.pat.n;
+    const bool f = fwd.precision != kFP64;
+    if (int rc0 = const_cast<Plan&>(fwd).ensure_device(err)) return rc0;
+    if (int rc0 = const_cast<Plan&>(bwd).ensure_device(err)) return rc0;
+    if (bwd.pat.n_sp != nf) { *err = "adjoint setpoint size differs from the forward state size"; return 1; }
+    if (sig.f32 != f) { *err = "signal table precision differs from the plan's"; return 1; }
+    if (B == 0) return 0;
+    if (nsteps < 1) { *err = "gradient needs at least one step"; return 1; }
+    const int S = (int)std::sqrt((double)nsteps);
+    const int C = (int)std::ceil((double)nsteps / (double)S);
+    const int lastC = C - (int)(((long long)S * C) % nsteps);
+    const long long slots = (long long)S + C - 1;
+    DevBuf dfv, dbv, dx0, da0, dexc, dtraj, dscr, dout, stage;
+    int rc = upload_interleaved(fvals, B, fwd.pat.P(), f, kHost, dfv, stage, st, err);
+    if (rc) return rc;
+    rc = upload_interleaved(bvals, B, bwd.pat.P(), f, kHost, dbv, stage, st, err);
+    if (rc) return rc;
+    rc = upload_interleaved(x0h, B, nf, f, kHost, dx0, stage, st, err);
+    if (rc) return rc;
+    rc = upload_interleaved(a0h, B, na, f, kHost, da0, stage, st, err);
+    if (rc) return rc;
+    for (int i = 0; i < B; ++i)
+        if (exc_index[i] < 0 || exc_index[i] >= sig.n_exc) { *err = "excitation index out of range"; return 1; }
+    const size_t rs = f ? sizeof(float) : sizeof(double);
+    PK_CUDA(dexc.ensure(sizeof(int) * B), "cudaMalloc");
+    PK_CUDA(cudaMemcpyAsync(dexc.p, exc_index, sizeof(int) * B, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    PK_CUDA(dtraj.ensure((size_t)slots * nf * B * rs), "cudaMalloc");
+    PK_CUDA(cudaMemsetAsync(dtraj.p, 0, (size_t)slots * nf * B * rs, st), "cudaMemsetAsync");
+    PK_CUDA(dscr.ensure((size_t)(5 * nf + 6 * na) * B * rs), "cudaMalloc");
+    PK_CUDA(dout.ensure((size_t)na * B * rs), "cudaMalloc");
+    cudaError_t e;
+#define PK_FILL_RG(R_)                          \
+    pk::RefGradArgs<R_> a;                      \
+    std::memset(&a, 0, sizeof(a));              \
+    a.fvals = dfv.as<R_>();                     \
+    a.bvals = dbv.as<R_>();                     \
+    a.x0 = dx0.as<R_>();                        \
+    a.a0 = da0.as<R_>();                        \
+    a.exc_index = dexc.as<int>();               \
+    a.traj = dtraj.as<R_>();                    \
+    a.scratch = dscr.as<R_>();                  \
+    a.out = dout.as<R_>();                      \
+    a.frc = sig.forcing<R_>();                  \
+    a.fgp = fwd.gen();                          \
+    a.bgp = bwd.gen();                          \
+    a.h = (R_)h;                                \
+    a.h2 = (R_)(h / 2.0);                       \
+    a.h6 = (R_)(h / 6.0);                       \
+    a.B = B;                                    \
+    a.nsteps = nsteps;                          \
+    a.S = S;                                    \
+    a.C = C;                                    \
+    a.lastC = lastC;                            \
+    a.save = save;                              \
+    a.slots = slots;
+    if (f) {
+        PK_FILL_RG(float)
+        e = pk::launch_gen_refgrad(a, st);
+    } else {
+        PK_FILL_RG(double)
+        e = pk::launch_gen_refgrad(a, st);
+    }
+#undef PK_FILL_RG
+    PK_CUDA(e, "gradient kernel launch");
+    return download_interleaved(dout.p, B, na, f, 1.0, out, kHost, stage, st, err);
+}
+
+}  // namespace pasif

@@ -1,0 +1,122 @@
+// engine.h -- batched RK4 engine: plans (pattern + precision), device signal
+// tables and device-resident batches of instances.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "jit.h"
+#include "pattern.h"
+#include "pk_args.h"
+
+namespace pasif {
+
+enum Precision { kFP64 = 0, kFP32 = 1, kFP32Kahan = 2 };
+enum Memory { kHost = 0, kDevice = 1 };
+enum KernelKind { kNone = 0, kGeneric = 1, kSpecialised = 2 };
+
+// Growable device allocation.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf();
+    cudaError_t ensure(size_t n);
+    void release();
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Excitation table in the compute precision (src/__GpuDriver.cu:343-381 keeps
+// it as reel on the device).
+struct Signals {
+    bool f32 = false;
+    int n_exc = 0;
+    int len = 0;
+    unsigned w = 0, lw = 0;
+    DevBuf x, im;
+    template <typename R> pk::Forcing<R> forcing() const {
+        pk::Forcing<R> f;
+        f.x = x.as<R>();
+        f.im = w ? im.as<R>() : nullptr;
+        f.total = (long long)n_exc * len;
+        f.len = (unsigned)len;
+        f.w = w;
+        f.lw = lw;
+        f.pad_ = 0;
+        return f;
+    }
+};
+
+// Build a signal table; x and im are host or device (memory) pointers.
+int signals_create(const double* x, int n_exc, int len, int window, const double* im, int precision,
+                   int memory, cudaStream_t st, std::shared_ptr<Signals>* out, std::string* err);
+
+struct Plan {
+    Pattern pat;
+    int precision = kFP64;
+    bool generic_only = false;
+    DevBuf gpat;            // flat pattern for the generic kernels (uploaded on first use)
+    pk::GenPattern gen() const;
+    int ensure_device(std::string* err);
+};
+
+int plan_create(const Pattern& pat, int precision, bool generic_only, std::shared_ptr<Plan>* out,
+                std::string* err);
+
+struct Reducers {
+    std::vector<int> max_comp;   // ascending, < 64
+    int max_start = 0;
+    std::vector<int> sq_comp;    // ascending, < 64
+    int sq_start = 0;
+};
+
+// Instances of one plan, resident on the device in [k][B] layout.
+struct Batch {
+    std::shared_ptr<Plan> plan;
+    int B = 0;
+    DevBuf vals, x0, state, exc, out_max, out_sq, scratch, stage, traj;
+    DevBuf ckpt, buf, pbar, dx0, gfin, gsq, adj_stage;
+    Literals lit;
+    int n_max = 0;
+    bool has_sq = false;
+    int max_exc_ = -1;
+    double last_h = 0.0;          // time step of the last forward (scales sum q^2)
+    int last_kind = kNone;
+    JitKernel last_jit;
+    std::string last_jit_error;
+
+    bool f32() const { return plan->precision != kFP64; }
+    size_t rsize() const { return f32() ? sizeof(float) : sizeof(double); }
+
+    // values[B][P], x0[B][n] (double), exc_index[B]; host or device pointers.
+    int set(const double* values, const double* x0h, const int* exc_index, int memory, cudaStream_t st,
+            std::string* err);
+    // Integrate nsteps from step0; trajectory (optional): every `traj_every`
+    // steps into an internal [slots][n][B] buffer.
+    int forward(const Signals& sig, double h, int step0, int nsteps, const Reducers& red, int traj_every,
+                long long traj_slots, cudaStream_t st, std::string* err);
+    // Results in [B][k] double order (host or device pointers; any may be null).
+    int get(double* state_out, double* max_out, double* sq_out, double h, int memory, cudaStream_t st,
+            std::string* err);
+    int get_traj(double* out, long long slots, int memory, cudaStream_t st, std::string* err);
+    // Exact discrete adjoint; g_final[B][n] and g_sq[B] may be null.
+    int adjoint(const Signals& sig, double h, int nsteps, const Reducers& red, const double* g_final,
+                const double* g_sq, double* d_values, double* d_x0, int memory, cudaStream_t st,
+                std::string* err);
+};
+
+int batch_create(std::shared_ptr<Plan> plan, int B, std::unique_ptr<Batch>* out, std::string* err);
+
+// __GpuDriver::_getGradient semantics for B instances of a (forward, adjoint)
+// pattern pair.  All arrays host, [B][k] double.  out[B][na].
+int refgrad_run(const Plan& fwd, const Plan& bwd, int B, const double* fvals, const double* bvals,
+                const double* x0, const double* a0, const int* exc_index, const Signals& sig, double h,
+                int nsteps, int save, double* out, cudaStream_t st, std::string* err);
+
+std::string cuda_err(const char* what, cudaError_t e);
+
+}  // namespace pasif

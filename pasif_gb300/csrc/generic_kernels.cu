@@ -1,0 +1,200 @@
+// generic_kernels.cu -- pattern-interpreting kernels (any sparsity pattern,
+// any state size), built by nvcc for sm_103a.  One thread owns one instance;
+// its work vectors live in a [k*n][B] scratch block (coalesced).  The
+// pattern-specialised NVRTC kernels (jit.cpp) are the fast path; these are
+// the path for patterns the specialiser does not take and the cross-check
+// of the specialiser.
+#include "generic_kernels.h"
+#include "rk4_core.cuh"
+
+namespace pk {
+
+template <typename R, bool KAHAN>
+__global__ void __launch_bounds__(128) gen_fwd(FwdArgs<R> a) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= a.B) return;
+    GenSys<R> sys{a.gp, a.vals, (long long)a.B, b};
+    const long long B = a.B, n = a.gp.n;
+    R* base = a.scratch + b;
+    GVec<R> Q{base, B}, Cm{base + n * B, B}, S{base + 2 * n * B, B}, K{base + 3 * n * B, B},
+        Mi{base + 4 * n * B, B}, Mx{base + 5 * n * B, B};
+    const bool hmax = a.max_mask != 0ull, hsq = a.sq_mask != 0ull, htraj = a.traj != nullptr;
+    if (htraj)
+        fwd_run<R, 0, KAHAN, true, true, true>(sys, a, b, a.max_mask, a.sq_mask, Q, Cm, S, K, Mi, Mx);
+    else if (hmax && hsq)
+        fwd_run<R, 0, KAHAN, true, true, false>(sys, a, b, a.max_mask, a.sq_mask, Q, Cm, S, K, Mi, Mx);
+    else if (hmax)
+        fwd_run<R, 0, KAHAN, true, false, false>(sys, a, b, a.max_mask, a.sq_mask, Q, Cm, S, K, Mi, Mx);
+    else if (hsq)
+        fwd_run<R, 0, KAHAN, false, true, false>(sys, a, b, a.max_mask, a.sq_mask, Q, Cm, S, K, Mi, Mx);
+    else
+        fwd_run<R, 0, KAHAN, false, false, false>(sys, a, b, a.max_mask, a.sq_mask, Q, Cm, S, K, Mi, Mx);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) gen_adj(AdjArgs<R> a) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= a.B) return;
+    GenSys<R> sys{a.gp, a.vals, (long long)a.B, b};
+    adj_run_generic<R>(sys, a, b);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) gen_refgrad(RefGradArgs<R> a) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= a.B) return;
+    GenSys<R> fs{a.fgp, a.fvals, (long long)a.B, b};
+    GenSys<R> bs{a.bgp, a.bvals, (long long)a.B, b};
+    refgrad_run_generic<R>(fs, bs, a, b);
+}
+
+static inline dim3 grid_for(int B) { return dim3((unsigned)((B + 127) / 128)); }
+
+cudaError_t launch_gen_fwd(const FwdArgs<double>& a, bool kahan, cudaStream_t st) {
+    if (a.B <= 0) return cudaSuccess;
+    if (kahan) gen_fwd<double, true><<<grid_for(a.B), 128, 0, st>>>(a);
+    else gen_fwd<double, false><<<grid_for(a.B), 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gen_fwd(const FwdArgs<float>& a, bool kahan, cudaStream_t st) {
+    if (a.B <= 0) return cudaSuccess;
+    if (kahan) gen_fwd<float, true><<<grid_for(a.B), 128, 0, st>>>(a);
+    else gen_fwd<float, false><<<grid_for(a.B), 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gen_adj(const AdjArgs<double>& a, cudaStream_t st) {
+    if (a.B <= 0) return cudaSuccess;
+    gen_adj<double><<<grid_for(a.B), 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gen_adj(const AdjArgs<float>& a, cudaStream_t st) {
+    if (a.B <= 0) return cudaSuccess;
+    gen_adj<float><<<grid_for(a.B), 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gen_refgrad(const RefGradArgs<double>& a, cudaStream_t st) {
+    if (a.B <= 0) return cudaSuccess;
+    gen_refgrad<double><<<grid_for(a.B), 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gen_refgrad(const RefGradArgs<float>& a, cudaStream_t st) {
+    if (a.B <= 0) return cudaSuccess;
+    gen_refgrad<float><<<grid_for(a.B), 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ---- layout kernels: host order [B][k] (double) <-> device order [k][B] (R)
+
+template <typename R>
+__global__ void to_interleaved(const double* __restrict__ src, R* __restrict__ dst, int B, int k) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)B * k;
+    if (t >= total) return;
+    const long long b = t / k, p = t % k;   // src read coalesced
+    dst[p * B + b] = (R)src[t];
+}
+
+template <typename R>
+__global__ void from_interleaved(const R* __restrict__ src, double* __restrict__ dst, int B, int k,
+                                 double scale) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)B * k;
+    if (t >= total) return;
+    const long long b = t / k, p = t % k;   // dst written coalesced
+    dst[t] = (double)src[p * B + b] * scale;
+}
+
+template <typename R>
+__global__ void convert_kernel(const double* __restrict__ src, R* __restrict__ dst, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (R)src[t];
+}
+
+static inline unsigned blocks_for(long long n) { return (unsigned)((n + 255) / 256); }
+
+cudaError_t launch_to_interleaved(const double* src, void* dst, int B, int k, bool f32, cudaStream_t st) {
+    const long long total = (long long)B * k;
+    if (total == 0) return cudaSuccess;
+    if (f32) to_interleaved<float><<<blocks_for(total), 256, 0, st>>>(src, (float*)dst, B, k);
+    else to_interleaved<double><<<blocks_for(total), 256, 0, st>>>(src, (double*)dst, B, k);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_interleaved(const void* src, double* dst, int B, int k, bool f32, cudaStream_t st,
+                                    double scale) {
+    const long long total = (long long)B * k;
+    if (total == 0) return cudaSuccess;
+    if (f32) from_interleaved<float><<<blocks_for(total), 256, 0, st>>>((const float*)src, dst, B, k, scale);
+    else from_interleaved<double><<<blocks_for(total), 256, 0, st>>>((const double*)src, dst, B, k, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert(const double* src, void* dst, long long n, bool f32, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    if (f32) convert_kernel<float><<<blocks_for(n), 256, 0, st>>>(src, (float*)dst, n);
+    else convert_kernel<double><<<blocks_for(n), 256, 0, st>>>(src, (double*)dst, n);
+    return cudaGetLastError();
+}
+
+}  // namespace pk
+
+// ---- FMA-pipe peak probe (roofline denominator for the FMA-bound kernels)
+
+namespace pk {
+
+template <typename T>
+__global__ void __launch_bounds__(256) fma_peak_kernel(T* out, int iters, T a, T b) {
+    T x0 = (T)threadIdx.x * (T)1e-3, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3;
+    T x4 = x0 + (T)4, x5 = x0 + (T)5, x6 = x0 + (T)6, x7 = x0 + (T)7;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+            x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+        }
+    }
+    const T s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == (T)-1) out[0] = s;   // never true; keeps the chains alive
+}
+
+cudaError_t measure_fma_peak(bool f32, double* flops_per_s) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    void* out = nullptr;
+    e = cudaMalloc(&out, 16);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    const int blocks = sms * 8, threads = 256;
+    const int iters = f32 ? 8192 : 256;
+    double best = 0.0;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(t0);
+        if (f32) fma_peak_kernel<float><<<blocks, threads>>>((float*)out, iters, 0.9999f, 1e-4f);
+        else fma_peak_kernel<double><<<blocks, threads>>>((double*)out, iters, 0.9999, 1e-4);
+        cudaEventRecord(t1);
+        e = cudaEventSynchronize(t1);
+        if (e != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        const double flops = 2.0 * 32.0 * iters * (double)blocks * threads;
+        if (rep > 0 && ms > 0.f) best = flops / (ms * 1e-3) > best ? flops / (ms * 1e-3) : best;
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaFree(out);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    *flops_per_s = best;
+    return e;
+}
+
+}  // namespace pk

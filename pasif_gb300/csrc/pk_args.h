@@ -1,0 +1,107 @@
+// pk_args.h -- kernel argument blocks shared by the host engine, the nvcc-built
+// generic kernels and the NVRTC-built pattern-specialised kernels.  Plain
+// structs of pointers and scalars only: the same text is compiled by g++,
+// nvcc and NVRTC, so the layouts agree by construction.
+#pragma once
+
+namespace pk {
+
+// Excitation table in the compute precision plus the forcing mode.
+// w == 0: sample and hold (src/kernels.cu:72-89); else window W = 2^lw
+// interpolation with weights im[0..2W) (src/kernels.cu:97-126).
+template <typename R>
+struct Forcing {
+    const R* x;          // [n_exc * len], one row per signal
+    const R* im;         // 2*W weights: row 0 next-sample, row 1 current-sample
+    long long total;     // n_exc * len
+    unsigned len;
+    unsigned w;
+    unsigned lw;
+    unsigned pad_;
+};
+
+// Generic (interpreted) pattern description: device array laid out as
+// k_ptr[n+1] | k_col[k] | g_idx[3g] | l_idx[4l] | p_idx[5p] | f_idx[f].
+struct GenPattern {
+    const int* data;
+    int n;
+    int n_sp;
+    int k_nnz, g_nnz, l_nnz, p_nnz, f_nnz;
+    int P;
+};
+
+// Forward integration of a batch: one instance per thread.
+template <typename R>
+struct FwdArgs {
+    const R* vals;              // [P][B] per-instance values (system-interleaved)
+    R* state;                   // [n][B] initial state in, final state out
+    const int* exc_index;       // [B]
+    R* scratch;                 // generic kernels: [6n][B] work vectors
+    R* out_max;                 // [n_max][B]
+    R* out_sq;                  // [B] raw sum of squares (times h on the host)
+    R* traj;                    // [slots][n][B] states after steps t with t % traj_every == 0
+    long long traj_slots;
+    int traj_every;
+    int pad_;
+    Forcing<R> frc;
+    GenPattern gp;              // generic kernels only
+    R h, h2, h6;
+    int B;
+    unsigned step0;
+    int nsteps;
+    int max_start;
+    int sq_start;
+    unsigned long long max_mask;   // components reduced by max |q|
+    unsigned long long sq_mask;    // components reduced by sum q^2
+};
+
+// Exact discrete adjoint of the RK4 map with sqrt(N) checkpoints.
+template <typename R>
+struct AdjArgs {
+    const R* vals;              // [P][B]
+    const R* x0;                // [n][B]
+    const int* exc_index;       // [B]
+    R* ckpt;                    // [nck][2n][B] state + compensation at steps k*C
+    R* buf;                     // [C][n][B] recomputed chunk states
+    R* scratch;                 // generic kernels: [16n][B]
+    double* pbar;               // [P][B] parameter gradients (FP64 accumulation)
+    R* dx0;                     // [n][B]
+    const R* g_final;           // [n][B] or null
+    const R* g_sq;              // [B] or null
+    Forcing<R> frc;
+    GenPattern gp;
+    R h, h2, h6;
+    int B;
+    int nsteps;
+    int C;
+    int nck;
+    int kahan;
+    int sq_start;
+    unsigned long long sq_mask;
+};
+
+// __GpuDriver::_getGradient semantics (see the oracle for the quirk list).
+template <typename R>
+struct RefGradArgs {
+    const R* fvals;             // [Pf][B]
+    const R* bvals;             // [Pb][B]
+    const R* x0;                // [nf][B]
+    const R* a0;                // [na][B]
+    const int* exc_index;       // [B]
+    R* traj;                    // [slots][nf][B]
+    R* scratch;                 // generic kernels: [8(nf+na)][B]
+    R* out;                     // [na][B]
+    Forcing<R> frc;
+    GenPattern fgp;
+    GenPattern bgp;
+    R h, h2, h6;
+    int B;
+    int nsteps;
+    int S;
+    int C;
+    int lastC;
+    int save;
+    long long slots;
+};
+
+}  // namespace pk

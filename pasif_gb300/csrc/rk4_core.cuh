@@ -1,0 +1,456 @@
+// rk4_core.cuh -- device-side building blocks of the batched RK4 engine.
+//
+// Compiled twice: by nvcc into the generic (pattern-interpreting) kernels of
+// generic_kernels.cu, and by NVRTC together with a generated, pattern-
+// specialised system struct (jit.cpp).  It therefore includes nothing but
+// pk_args.h.
+//
+// Every floating-point operation on the solution path is an explicit
+// round-to-nearest intrinsic (__fma_rn, __dmul_rn, ...): the compiler may not
+// fuse or reorder them, and the operation order is the canonical one of the
+// CPU oracle (per destination: CSR row of K, then Gamma, Lambda, Psi entries
+// in COO order, then forcing; fma-folded from +0).  This is the order the
+// reference's kernels sum in, minus its atomicAdd nondeterminism
+// (src/kernels.cu:22-64, src/__GpuDriver.cu:785-838).
+#pragma once
+#include "pk_args.h"
+
+namespace pk {
+
+template <typename R> struct M;
+
+template <> struct M<double> {
+    static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double abs(double a) { return fabs(a); }
+    static __device__ __forceinline__ double max(double a, double b) { return fmax(a, b); }
+};
+
+template <> struct M<float> {
+    static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float abs(float a) { return fabsf(a); }
+    static __device__ __forceinline__ float max(float a, float b) { return fmaxf(a, b); }
+};
+
+// Register-resident vector (pattern-specialised kernels: every index is a
+// compile-time constant after unrolling).
+template <typename R, int N>
+struct RegVec {
+    R v[N];
+    __device__ __forceinline__ R& operator[](int i) { return v[i]; }
+    __device__ __forceinline__ const R& operator[](int i) const { return v[i]; }
+};
+
+// Strided vector in global memory, one element per system (coalesced when
+// consecutive threads own consecutive systems).
+template <typename R>
+struct GVec {
+    R* p;
+    long long s;
+    __device__ __forceinline__ R& operator[](int i) const { return p[(long long)i * s]; }
+};
+
+// Excitation seen by a stage at (step, off, half); src/kernels.cu:72-89 and
+// src/kernels.cu:97-126.  Sample 0 and samples >= len give no force; the
+// j+1 neighbour is read from the flat table (it crosses into the next signal
+// at j = len-1, as in the reference) and reads 0 past its end.
+template <typename R>
+__device__ __forceinline__ R force_at(const Forcing<R>& f, long long ebase, unsigned step,
+                                      unsigned off, unsigned half) {
+    if (f.w == 0u) {
+        const unsigned st = step + off;
+        return (st < f.len && st > 0u) ? f.x[ebase + st] : R(0);
+    }
+    const unsigned s2 = ((step + off) << 1) + half;
+    const unsigned idx = s2 & (f.w - 1u);
+    const unsigned j = s2 >> f.lw;
+    if (j < f.len && j > 0u) {
+        const long long base = ebase + j;
+        const R x0 = f.x[base];
+        const R x1 = (base + 1 < f.total) ? f.x[base + 1] : R(0);
+        const R wn = f.im[idx];
+        const R wc = f.im[f.w + idx];
+        return M<R>::fma(wc, x0, M<R>::mul(wn, x1));
+    }
+    return R(0);
+}
+
+// Pattern interpreted from GenPattern, values read from vals[p][B].
+template <typename R>
+struct GenSys {
+    GenPattern g;
+    const R* vals;
+    long long B;
+    int b;
+
+    __device__ __forceinline__ int dim() const { return g.n; }
+    __device__ __forceinline__ R val(int p) const { return vals[(long long)p * B + b]; }
+
+    // f = K.xs + Gamma:(xs,xp) + Lambda:(xs,xp,xp) + Psi:(xs,xp,xp,xp) [+ F u]
+    template <bool FORCE, class V, class W, class F>
+    __device__ __noinline__ void rhs(const V& xs, const W& xp, R u, F& f) const {
+        typedef M<R> m;
+        const int* kp = g.data;
+        const int* kc = kp + g.n + 1;
+        const int* gi = kc + g.k_nnz;
+        const int* li = gi + 3 * g.g_nnz;
+        const int* pi = li + 4 * g.l_nnz;
+        const int* fi = pi + 5 * g.p_nnz;
+        for (int i = 0; i < g.n; ++i) {
+            R acc = R(0);
+            for (int p = kp[i]; p < kp[i + 1]; ++p) acc = m::fma(val(p), xs[kc[p]], acc);
+            f[i] = acc;
+        }
+        int off = g.k_nnz;
+        for (int e = 0; e < g.g_nnz; ++e) {
+            const int* ix = gi + 3 * e;
+            f[ix[0]] = m::fma(m::mul(val(off + e), xs[ix[1]]), xp[ix[2]], f[ix[0]]);
+        }
+        off += g.g_nnz;
+        for (int e = 0; e < g.l_nnz; ++e) {
+            const int* ix = li + 4 * e;
+            const R t = m::mul(m::mul(val(off + e), xs[ix[1]]), xp[ix[2]]);
+            f[ix[0]] = m::fma(t, xp[ix[3]], f[ix[0]]);
+        }
+        off += g.l_nnz;
+        for (int e = 0; e < g.p_nnz; ++e) {
+            const int* ix = pi + 5 * e;
+            const R t = m::mul(m::mul(m::mul(val(off + e), xs[ix[1]]), xp[ix[2]]), xp[ix[3]]);
+            f[ix[0]] = m::fma(t, xp[ix[4]], f[ix[0]]);
+        }
+        off += g.p_nnz;
+        if (FORCE)
+            for (int e = 0; e < g.f_nnz; ++e) f[fi[e]] = m::fma(val(off + e), u, f[fi[e]]);
+    }
+
+    // out = J(y)^T w ; pb += (df/dp)^T w  (forward systems: xs == xp == y).
+    template <class V, class W, class O, class PB>
+    __device__ __noinline__ void vjp(const V& y, const W& w, R u, O& out, PB& pb) const {
+        typedef M<R> m;
+        const int* kp = g.data;
+        const int* kc = kp + g.n + 1;
+        const int* gi = kc + g.k_nnz;
+        const int* li = gi + 3 * g.g_nnz;
+        const int* pi = li + 4 * g.l_nnz;
+        const int* fi = pi + 5 * g.p_nnz;
+        for (int i = 0; i < g.n; ++i) out[i] = R(0);
+        for (int i = 0; i < g.n; ++i) {
+            const R wi = w[i];
+            for (int p = kp[i]; p < kp[i + 1]; ++p) {
+                const int j = kc[p];
+                out[j] = m::fma(val(p), wi, out[j]);
+                pb[p] = __fma_rn((double)wi, (double)y[j], pb[p]);
+            }
+        }
+        int off = g.k_nnz;
+        for (int e = 0; e < g.g_nnz; ++e) {
+            const int* ix = gi + 3 * e;
+            const R wi = w[ix[0]], yj = y[ix[1]], yk = y[ix[2]];
+            const R a = m::mul(val(off + e), wi);
+            out[ix[1]] = m::fma(a, yk, out[ix[1]]);
+            out[ix[2]] = m::fma(a, yj, out[ix[2]]);
+            pb[off + e] = __fma_rn((double)m::mul(wi, yj), (double)yk, pb[off + e]);
+        }
+        off += g.g_nnz;
+        for (int e = 0; e < g.l_nnz; ++e) {
+            const int* ix = li + 4 * e;
+            const R wi = w[ix[0]], yj = y[ix[1]], yk = y[ix[2]], yl = y[ix[3]];
+            const R a = m::mul(val(off + e), wi);
+            out[ix[1]] = m::fma(m::mul(a, yk), yl, out[ix[1]]);
+            out[ix[2]] = m::fma(m::mul(a, yj), yl, out[ix[2]]);
+            out[ix[3]] = m::fma(m::mul(a, yj), yk, out[ix[3]]);
+            pb[off + e] = __fma_rn((double)m::mul(m::mul(wi, yj), yk), (double)yl, pb[off + e]);
+        }
+        off += g.l_nnz;
+        for (int e = 0; e < g.p_nnz; ++e) {
+            const int* ix = pi + 5 * e;
+            const R wi = w[ix[0]], yj = y[ix[1]], yk = y[ix[2]], yl = y[ix[3]], ym = y[ix[4]];
+            const R a = m::mul(val(off + e), wi);
+            out[ix[1]] = m::fma(m::mul(m::mul(a, yk), yl), ym, out[ix[1]]);
+            out[ix[2]] = m::fma(m::mul(m::mul(a, yj), yl), ym, out[ix[2]]);
+            out[ix[3]] = m::fma(m::mul(m::mul(a, yj), yk), ym, out[ix[3]]);
+            out[ix[4]] = m::fma(m::mul(m::mul(a, yj), yk), yl, out[ix[4]]);
+            pb[off + e] = __fma_rn((double)m::mul(m::mul(m::mul(wi, yj), yk), yl), (double)ym, pb[off + e]);
+        }
+        off += g.p_nnz;
+        for (int e = 0; e < g.f_nnz; ++e)
+            pb[off + e] = __fma_rn((double)w[fi[e]], (double)u, pb[off + e]);
+    }
+};
+
+// One RK4 step (src/__GpuDriver.cu:693-713): k1 at u(step, half 0), k2 and k3
+// at u(step, half 1), k4 at u(step+1, half 0); Q += h/6 (k1 + 2k2 + 2k3 + k4)
+// with the sum formed as ((k1 + 2k2) + 2k3) + k4.  KAHAN: compensated update.
+// N > 0: compile-time size (registers); N == 0: runtime size sys.dim().
+template <typename R, int N, bool KAHAN, class Sys, class V>
+__device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K, V& Mi,
+                                         R ua, R ub, R uc, R h, R h2, R h6) {
+    typedef M<R> m;
+    const int n = N ? N : sys.dim();
+    sys.template rhs<true>(Q, Q, ua, K);
+#pragma unroll
+    for (int i = 0; i < n; ++i) { S[i] = K[i]; Mi[i] = m::fma(h2, K[i], Q[i]); }
+    sys.template rhs<true>(Mi, Mi, ub, K);
+#pragma unroll
+    for (int i = 0; i < n; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(h2, K[i], Q[i]); }
+    sys.template rhs<true>(Mi, Mi, ub, K);
+#pragma unroll
+    for (int i = 0; i < n; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(h, K[i], Q[i]); }
+    sys.template rhs<true>(Mi, Mi, uc, K);
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+        const R sum = m::add(S[i], K[i]);
+        if (KAHAN) {
+            const R inc = m::mul(h6, sum);
+            const R y = m::sub(inc, Cm[i]);
+            const R t = m::add(Q[i], y);
+            Cm[i] = m::sub(m::sub(t, Q[i]), y);
+            Q[i] = t;
+        } else {
+            Q[i] = m::fma(h6, sum, Q[i]);
+        }
+    }
+}
+
+// Forward integration of one instance with the max |q| and sum q^2 reducers.
+template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, class Sys, class V>
+__device__ __forceinline__ void fwd_run(const Sys& sys, const FwdArgs<R>& a, int b,
+                                        unsigned long long max_mask, unsigned long long sq_mask,
+                                        V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx) {
+    typedef M<R> m;
+    const int n = N ? N : sys.dim();
+    const long long B = a.B;
+    const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+        Q[i] = a.state[i * B + b];
+        if (KAHAN) Cm[i] = R(0);
+        if (HMAX) Mx[i] = R(0);
+    }
+    R sq = R(0), sqc = R(0);
+    R uc = force_at(a.frc, ebase, a.step0, 0u, 0u);
+    for (int s = 0; s < a.nsteps; ++s) {
+        const unsigned step = a.step0 + (unsigned)s;
+        const R ua = uc;
+        const R ub = force_at(a.frc, ebase, step, 0u, 1u);
+        uc = force_at(a.frc, ebase, step, 1u, 0u);
+        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+        if (HTRAJ && step % (unsigned)a.traj_every == 0u) {
+            const long long slot = (long long)(step / (unsigned)a.traj_every) - (long long)(a.step0 / (unsigned)a.traj_every)
+                                   - ((a.step0 % (unsigned)a.traj_every) ? 1 : 0);
+            if (slot >= 0 && slot < a.traj_slots) {
+#pragma unroll
+                for (int i = 0; i < n; ++i) a.traj[(slot * n + i) * B + b] = Q[i];
+            }
+        }
+        if (HMAX && (long long)step >= (long long)a.max_start) {
+#pragma unroll
+            for (int i = 0; i < n; ++i)
+                if (i < 64 && ((max_mask >> i) & 1ull)) Mx[i] = m::max(Mx[i], m::abs(Q[i]));
+        }
+        if (HSQ && (long long)step >= (long long)a.sq_start) {
+#pragma unroll
+            for (int i = 0; i < n; ++i)
+                if (i < 64 && ((sq_mask >> i) & 1ull)) {
+                    const R q = Q[i];
+                    if (KAHAN) {
+                        const R y = m::sub(m::mul(q, q), sqc);
+                        const R t = m::add(sq, y);
+                        sqc = m::sub(m::sub(t, sq), y);
+                        sq = t;
+                    } else {
+                        sq = m::fma(q, q, sq);
+                    }
+                }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < n; ++i) a.state[i * B + b] = Q[i];
+    if (HMAX) {
+        int slot = 0;
+#pragma unroll
+        for (int i = 0; i < n; ++i)
+            if (i < 64 && ((max_mask >> i) & 1ull)) { a.out_max[slot * B + b] = Mx[i]; ++slot; }
+    }
+    if (HSQ) a.out_sq[b] = sq;
+}
+
+// Exact discrete adjoint of the RK4 map for one instance (generic storage):
+// forward pass with checkpoints every C steps (state and Kahan compensation
+// before step k*C), then per chunk in reverse: recompute the chunk's states
+// into buf and sweep backward.  The reverse of one step, with lam = dL/dQ_{s+1}:
+//   kb4 = h/6 lam, kb3 = kb2 = 2 h/6 lam, kb1 = h/6 lam
+//   yb4 = J(Y4)^T kb4; kb3 += h  yb4
+//   yb3 = J(Y3)^T kb3; kb2 += h/2 yb3
+//   yb2 = J(Y2)^T kb2; kb1 += h/2 yb2
+//   yb1 = J(Q)^T  kb1; lam_s = lam + yb4 + yb3 + yb2 + yb1
+// with parameter gradients accumulated in FP64 at every VJP.
+template <typename R, class Sys>
+__device__ void adj_run_generic(const Sys& sys, const AdjArgs<R>& a, int b) {
+    typedef M<R> m;
+    const int n = sys.dim();
+    const long long B = a.B;
+    R* base = a.scratch + b;
+    GVec<R> Q{base, B}, Cm{base + (long long)n * B, B}, S{base + 2LL * n * B, B},
+        K{base + 3LL * n * B, B}, Mi{base + 4LL * n * B, B}, Y2{base + 5LL * n * B, B},
+        Y3{base + 6LL * n * B, B}, Y4{base + 7LL * n * B, B}, LAM{base + 8LL * n * B, B},
+        QB{base + 9LL * n * B, B}, KB{base + 10LL * n * B, B}, YB{base + 11LL * n * B, B},
+        QN{base + 12LL * n * B, B};
+    GVec<double> PB{a.pbar + b, B};
+    const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+    const int P = sys.g.P;
+    for (int p = 0; p < P; ++p) PB[p] = 0.0;
+    for (int i = 0; i < n; ++i) { Q[i] = a.x0[i * B + b]; Cm[i] = R(0); }
+    // forward pass with checkpoints
+    for (int t = 0; t < a.nsteps; ++t) {
+        if (t % a.C == 0) {
+            R* ck = a.ckpt + (long long)(t / a.C) * 2 * n * B + b;
+            for (int i = 0; i < n; ++i) { ck[i * B] = Q[i]; ck[(n + i) * B] = Cm[i]; }
+        }
+        const unsigned st = (unsigned)t;
+        const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+        const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+        const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+        if (a.kahan) rk4_step<R, 0, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+        else rk4_step<R, 0, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+    }
+    for (int i = 0; i < n; ++i) LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0);
+    const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
+    for (int k = a.nck - 1; k >= 0; --k) {
+        const int start = k * a.C;
+        const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
+        const R* ck = a.ckpt + (long long)k * 2 * n * B + b;
+        for (int i = 0; i < n; ++i) { Q[i] = ck[i * B]; Cm[i] = ck[(n + i) * B]; }
+        for (int t = start; t < end; ++t) {
+            R* bt = a.buf + (long long)(t - start) * n * B + b;
+            for (int i = 0; i < n; ++i) bt[i * B] = Q[i];
+            const unsigned st = (unsigned)t;
+            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            if (a.kahan) rk4_step<R, 0, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+            else rk4_step<R, 0, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+        }
+        for (int i = 0; i < n; ++i) QN[i] = Q[i];
+        for (int t = end - 1; t >= start; --t) {
+            GVec<R> QC{a.buf + (long long)(t - start) * n * B + b, B};
+            if (a.g_sq && t >= a.sq_start)
+                for (int i = 0; i < n; ++i)
+                    if (i < 64 && ((a.sq_mask >> i) & 1ull)) LAM[i] = m::fma(gsq2h, QN[i], LAM[i]);
+            const unsigned st = (unsigned)t;
+            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            sys.template rhs<true>(QC, QC, ua, K);
+            for (int i = 0; i < n; ++i) Y2[i] = m::fma(a.h2, K[i], QC[i]);
+            sys.template rhs<true>(Y2, Y2, ub, K);
+            for (int i = 0; i < n; ++i) Y3[i] = m::fma(a.h2, K[i], QC[i]);
+            sys.template rhs<true>(Y3, Y3, ub, K);
+            for (int i = 0; i < n; ++i) Y4[i] = m::fma(a.h, K[i], QC[i]);
+            // kb4 = sb; qb = lam
+            for (int i = 0; i < n; ++i) { KB[i] = m::mul(a.h6, LAM[i]); QB[i] = LAM[i]; }
+            sys.vjp(Y4, KB, uc, YB, PB);
+            for (int i = 0; i < n; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h, YB[i], m::mul(R(2), sb));
+            }
+            sys.vjp(Y3, KB, ub, YB, PB);
+            for (int i = 0; i < n; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h2, YB[i], m::mul(R(2), sb));
+            }
+            sys.vjp(Y2, KB, ub, YB, PB);
+            for (int i = 0; i < n; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h2, YB[i], sb);
+            }
+            sys.vjp(QC, KB, ua, YB, PB);
+            for (int i = 0; i < n; ++i) { LAM[i] = m::add(QB[i], YB[i]); QN[i] = QC[i]; }
+        }
+    }
+    for (int i = 0; i < n; ++i) a.dx0[i * B + b] = LAM[i];
+}
+
+// __GpuDriver::_getGradient for one instance; the literal buffer simulation
+// of the oracle (checkpoint slots, chunk recompute, frozen scratch slot T).
+template <typename R, class FSys, class BSys>
+__device__ void refgrad_run_generic(const FSys& fs, const BSys& bs, const RefGradArgs<R>& a, int b) {
+    typedef M<R> m;
+    const int nf = fs.dim(), na = bs.dim();
+    const long long B = a.B;
+    R* base = a.scratch + b;
+    GVec<R> Q{base, B}, Cm{base + (long long)nf * B, B}, S{base + 2LL * nf * B, B},
+        K{base + 3LL * nf * B, B}, Mi{base + 4LL * nf * B, B};
+    R* ab = base + 5LL * nf * B;
+    GVec<R> A{ab, B}, M1{ab + (long long)na * B, B}, M2{ab + 2LL * na * B, B},
+        M3{ab + 3LL * na * B, B}, M4{ab + 4LL * na * B, B}, MI{ab + 5LL * na * B, B};
+    const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+    const long long slotstride = (long long)nf * B;
+    R* tr = a.traj + b;
+    const int N = a.nsteps, C = a.C;
+    for (int i = 0; i < nf; ++i) Q[i] = a.x0[i * B + b];
+    long long idx = 0;
+    for (int t = 0; t < N; ++t) {
+        const unsigned st = (unsigned)t;
+        rk4_step<R, 0, false>(fs, Q, Cm, S, K, Mi, force_at(a.frc, ebase, st, 0u, 0u),
+                              force_at(a.frc, ebase, st, 0u, 1u), force_at(a.frc, ebase, st, 1u, 0u),
+                              a.h, a.h2, a.h6);
+        if (t % C == 0) {
+            for (int i = 0; i < nf; ++i) tr[idx * slotstride + (long long)i * B] = Q[i];
+            ++idx;
+        }
+    }
+    for (int i = 0; i < na; ++i) A[i] = a.a0[i * B + b];
+    long long T = -1;
+    for (long long sp = a.S - 1; sp >= 1; --sp) {
+        const long long start = sp * C;
+        long long end, sb;
+        if (sp == a.S - 1) { end = N; sb = sp + (a.lastC - 1); }
+        else { end = start + C; sb = sp + (C - 1); }
+        for (int i = 0; i < nf; ++i) Q[i] = tr[sp * slotstride + (long long)i * B];
+        idx = 0;
+        for (long long t = start; t < end; ++t) {
+            const unsigned st = (unsigned)t;
+            rk4_step<R, 0, false>(fs, Q, Cm, S, K, Mi, force_at(a.frc, ebase, st, 0u, 0u),
+                                  force_at(a.frc, ebase, st, 0u, 1u), force_at(a.frc, ebase, st, 1u, 0u),
+                                  a.h, a.h2, a.h6);
+            for (int i = 0; i < nf; ++i) tr[(idx + sp) * slotstride + (long long)i * B] = Q[i];
+            ++idx;
+        }
+        if (T < 0) T = sb;
+        long long spc = sb;
+        GVec<R> TG{tr + T * slotstride, B};
+        for (long long t = end - 1; t >= start; --t) {
+            GVec<R> CUR{tr + spc * slotstride, B}, PRV{tr + (spc - 1) * slotstride, B};
+            for (int i = 0; i < nf; ++i) TG[i] = CUR[i];
+            bs.template rhs<false>(A, TG, R(0), M1);
+            for (int i = 0; i < na; ++i) MI[i] = m::fma(a.h2, M1[i], A[i]);
+            for (int i = 0; i < nf; ++i) TG[i] = m::mul(R(0.5), m::add(CUR[i], PRV[i]));
+            bs.template rhs<false>(MI, TG, R(0), M2);
+            for (int i = 0; i < na; ++i) MI[i] = m::fma(a.h2, M2[i], A[i]);
+            bs.template rhs<false>(MI, TG, R(0), M3);
+            for (int i = 0; i < na; ++i) MI[i] = m::fma(a.h, M3[i], A[i]);
+            for (int i = 0; i < nf; ++i) TG[i] = PRV[i];
+            bs.template rhs<false>(MI, TG, R(0), M4);
+            for (int i = 0; i < na; ++i) {
+                R sum = m::fma(R(2), M2[i], M1[i]);
+                sum = m::fma(R(2), M3[i], sum);
+                sum = m::add(sum, M4[i]);
+                A[i] = m::fma(a.h6, sum, A[i]);
+            }
+            --spc;
+        }
+        if (sp == a.save) break;
+    }
+    for (int i = 0; i < na; ++i) a.out[i * B + b] = A[i];
+}
+
+}  // namespace pk

@@ -1,0 +1,61 @@
+"""Exact discrete adjoint on the GPU vs the oracle's adjoint (bit for bit in
+FP64) and vs central finite differences of the GPU forward."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from pasif_gb300 import synth
+from pasif_gb300.batch import Batch, Plan, Signals
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_adjoint(pat, vals, x0, exc, x, h, N, W, im, prec, gf, gs, sq_comp, sq_start):
+    plan = Plan(pat, prec)
+    b = Batch(plan, vals, x0, exc)
+    return b.adjoint(Signals(x, W, im, prec), h, N, g_final=gf, g_sq=gs, sq_comp=sq_comp, sq_start=sq_start)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_adjoint_bit_exact_fp64(gpu, seed):
+    rng = np.random.default_rng(300 + seed)
+    pat, v = cases.random_system(rng)
+    B = 40
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    x = cases.signals(rng, 2, 120)
+    exc = rng.integers(0, 2, B)
+    N = [50, 97, 144][seed]
+    gf = rng.normal(size=(B, pat.n))
+    gs = rng.normal(size=B)
+    sq = (0,)
+    dv, dx = gpu_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, [[0, .5], [1, .5]], "fp64", gf, gs, sq, N // 3)
+    odv, odx = O.batch_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, [[0, .5], [1, .5]], gf, gs, sq, N // 3)
+    np.testing.assert_array_equal(dv, odv)
+    np.testing.assert_array_equal(dx, odx)
+
+
+def test_adjoint_config3_fd_and_fp32(gpu):
+    w = synth.chain8(n_sys=8, nsteps=3000)
+    B = w.n_sys
+    gs = np.ones(B)
+    args = (w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im)
+    dv, _ = gpu_adjoint(*args, "fp64", None, gs, w.sq_comp, w.sq_start)
+    # central differences of the GPU forward on a few parameters of system 0
+    plan = Plan(w.pattern, "fp64")
+    sig = Signals(w.signals, w.window, w.im, "fp64")
+    eps = 1e-6
+    for q in (0, 9, 20, w.pattern.offsets()["Gamma"], w.pattern.offsets()["Lambda"] + 3):
+        vp, vm = w.values.copy(), w.values.copy()
+        vp[0, q] += eps
+        vm[0, q] -= eps
+        out = []
+        for vv in (vp, vm):
+            b = Batch(plan, vv, w.x0, w.exc_index)
+            b.forward(sig, w.h, w.nsteps, sq_comp=w.sq_comp, sq_start=w.sq_start)
+            out.append(b.get()[2][0])
+        fd = (out[0] - out[1]) / (2 * eps)
+        assert dv[0, q] == pytest.approx(fd, rel=1e-6, abs=1e-9)
+    dv32, _ = gpu_adjoint(*args, "fp32_kahan", None, gs, w.sq_comp, w.sq_start)
+    rel = np.abs(dv32 - dv) / (np.abs(dv) + 1e-3 * np.abs(dv).max())
+    assert rel.max() < 1e-4

@@ -1,0 +1,152 @@
+"""The __GpuDriver drop-in (and the PASIf front end above it) on the GPU vs the
+oracle's restatement of _getAmplitudes / _getTrajectory / _getGradient on the
+same concatenated system."""
+import numpy as np
+import pytest
+from scipy.sparse import coo_matrix, dia_matrix
+
+from oracle import pyoracle as O
+from pasif_gb300.frontend import PASIf, coo_tensor
+from pasif_gb300.system import Pattern
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_system(K_csr, gam, lam, force, psi=None, n_sp=None):
+    """Pattern + values of a concatenated system as the driver receives it."""
+    n = K_csr.shape[0]
+    fi = [i for i, v in enumerate(force) if abs(v) > np.finfo(float).eps]
+    g = np.asarray(gam.indices, np.int32).reshape(-1, 3)
+    l = np.asarray(lam.indices, np.int32).reshape(-1, 4)
+    p = np.asarray(psi.indices, np.int32).reshape(-1, 5) if psi is not None else np.zeros((0, 5), np.int32)
+    pat = Pattern(n=n, k_ptr=K_csr.indptr, k_col=K_csr.indices, g_idx=g, l_idx=l, p_idx=p, f_idx=fi, n_sp=n_sp or n)
+    vals = np.concatenate([K_csr.data, np.asarray(gam.val, float), np.asarray(lam.val, float),
+                           np.asarray(psi.val, float) if psi is not None else [], np.asarray(force)[fi]])
+    return pat, vals
+
+
+def probe_system():
+    c = cases.one_dof_probe()
+    M = dia_matrix(([1., 1., 1., 1.], [0]), shape=(4, 4))
+    B = coo_matrix(([-1., -1.], ([0, 1], [2, 3])), shape=(4, 4))
+    K = coo_matrix(([1.0, 1.0], ([2, 2], [0, 2])), shape=(4, 4))
+    G = coo_tensor([4, 4, 4]); G.val = [-1.]; G.indices = [3, 0, 0]
+    L = coo_tensor([4, 4, 4, 4]); L.val = [0]; L.indices = [0, 0, 0, 0]
+    return M, B, K, G, L, np.array([0., 0., 1., 0.]), np.zeros(4)
+
+
+def random_user_system(rng, n):
+    M = dia_matrix((rng.uniform(0.5, 2.0, n), [0]), shape=(n, n))
+    pat, v = cases.random_system(rng, n, with_psi=False)
+    rows = np.repeat(np.arange(n), np.diff(pat.k_ptr))
+    kv = v[:pat.k_nnz]
+    Bm = coo_matrix((kv[::2], (rows[::2], pat.k_col[::2])), shape=(n, n))
+    Km = coo_matrix((kv[1::2], (rows[1::2], pat.k_col[1::2])), shape=(n, n))
+    o = pat.offsets()
+    G = coo_tensor([n, n, n]); G.val = list(v[o["Gamma"]:o["Lambda"]]); G.indices = pat.g_idx.reshape(-1).tolist()
+    L = coo_tensor([n, n, n, n]); L.val = list(v[o["Lambda"]:o["Psi"]]); L.indices = pat.l_idx.reshape(-1).tolist()
+    F = np.zeros(n); F[pat.f_idx] = v[o["F"]:o["end"]]
+    return M, Bm, Km, G, L, F, rng.normal(0, 0.2, n)
+
+
+def build(rng, E=3, L=120, numsteps=150, interp=None, precision="fp64"):
+    exc = [np.sin(0.05 * (e + 1) * np.arange(L)) + 0.1 * rng.standard_normal(L) for e in range(E)]
+    p = PASIf(exc, 64, numsteps, precision=precision)
+    systems = [probe_system(), random_user_system(rng, 3), probe_system(), random_user_system(rng, 2)]
+    p.setSystems(*[list(z) for z in zip(*systems)])
+    if interp is not None:
+        p.setInterpolationMatrix(interp)
+    return p, np.asarray(exc)
+
+
+def test_amplitudes_bit_exact(gpu):
+    rng = np.random.default_rng(21)
+    p, exc = build(rng)
+    got = np.asarray(p.getAmplitudes())
+    K, Gam, Lam, F, IC = p.getMatrices()
+    csr = K.tocsr(); csr.sort_indices()
+    pat, vals = oracle_system(csr, Gam, Lam, F)
+    ref = O.get_amplitudes(pat, vals, IC, exc, 1 / 64, 150)
+    assert got.shape == ref.shape == (3 * pat.n,)
+    np.testing.assert_array_equal(got, ref)
+    assert p._lastKernel() == "specialised"
+    # a second call starts from the initial conditions again (resetStatesVectors)
+    np.testing.assert_array_equal(np.asarray(p.getAmplitudes()), ref)
+
+
+def test_amplitudes_with_interpolation_matrix(gpu):
+    rng = np.random.default_rng(22)
+    W = 8
+    im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W])
+    p, exc = build(rng, L=40, numsteps=200, interp=im)   # 200 steps > 40 samples * 4: gated tail
+    got = np.asarray(p.getAmplitudes())
+    K, Gam, Lam, F, IC = p.getMatrices()
+    csr = K.tocsr(); csr.sort_indices()
+    pat, vals = oracle_system(csr, Gam, Lam, F)
+    ref = O.get_amplitudes(pat, vals, IC, exc, 1 / 64, 200, W, im)
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_trajectory(gpu):
+    rng = np.random.default_rng(23)
+    p, exc = build(rng, numsteps=90)
+    K, Gam, Lam, F, IC = p.getMatrices()
+    csr = K.tocsr(); csr.sort_indices()
+    pat, vals = oracle_system(csr, Gam, Lam, F)
+    for save in (1, 4, 7):
+        got = np.asarray(p._getTrajectory(save))
+        ref = O.get_trajectory(pat, vals, IC, exc, 1 / 64, 90, save)
+        np.testing.assert_array_equal(got, ref)
+    tr = p.getTrajectory(3)
+    assert tr.shape == (pat.n * 3 + 1, 30)
+
+
+def adjoint_inputs():
+    c = cases.one_dof_probe()
+    n = 6
+    M = dia_matrix((np.ones(n), [0]), shape=(n, n))
+    B = coo_matrix(([-1, -1], ([1, 2], [4, 5])), shape=(n, n))
+    K = coo_matrix(([], ([], [])), shape=(n, n))
+    G = coo_tensor([n, n, 4]); G.val = []; G.indices = []
+    L = coo_tensor([n, n, 4, 4]); L.val = [-1, -1]; L.indices = [4, 0, 0, 0, 5, 0, 1, 1]
+    Psi = coo_tensor([n, n, 4, 4, 4]); Psi.val = [0]; Psi.indices = [1, 1, 1, 1, 1]
+    return M, B, K, G, L, np.zeros(n), c["a0"].copy(), Psi
+
+
+def test_gradient_reference_semantics(gpu):
+    rng = np.random.default_rng(24)
+    E, L = 2, 140
+    exc = [1.0 + 0.2 * rng.standard_normal(L) for _ in range(E)]
+    N = 117
+    p = PASIf(exc, 16, N)
+    sysl = [probe_system(), probe_system()]
+    p.setSystems(*[list(z) for z in zip(*sysl)])
+    adj = [adjoint_inputs(), adjoint_inputs()]
+    p.setJacobian(*[list(z) for z in zip(*adj)])
+    got = np.asarray(p.getGradient())
+    K, Gam, Lam, F, IC = p.getMatrices()
+    csr = K.tocsr(); csr.sort_indices()
+    fpat, fvals = oracle_system(csr, Gam, Lam, F)
+    bcsr = (p.jacobian_B + p.jacobian_K).tocsr(); bcsr.sort_indices()
+    bpat, bvals = oracle_system(bcsr, p.jacobian_Gamma, p.jacobian_Lambda, p.jacobian_forcePattern, p.jacobian_Psi,
+                                n_sp=fpat.n)
+    a0 = np.asarray(p.jacobian_initialConditions, float)
+    ref = O.get_gradient(fpat, fvals, IC, bpat, bvals, a0, np.asarray(exc), 1 / 16, N)
+    np.testing.assert_array_equal(got, ref)
+    # the terminal condition is chained into the next call (src/__GpuDriver.cu:743)
+    got2 = np.asarray(p.getGradient())
+    ref2 = np.concatenate([O.get_gradient(fpat, fvals, IC, bpat, bvals, ref[e * 12:(e + 1) * 12],
+                                          np.asarray(exc)[e:e + 1], 1 / 16, N) for e in range(E)])
+    np.testing.assert_array_equal(got2, ref2)
+
+
+def test_error_behaviour(gpu):
+    p = PASIf([np.ones(10), np.ones(10)], 16, 5)
+    with pytest.raises(ValueError):
+        p.getAmplitudes()
+    assert p._loadExcitationsSet([np.ones(10), np.ones(9)], 16) == 1
+    with pytest.raises(RuntimeError):
+        p._getAmplitudes()
+    with pytest.raises(ValueError):
+        p._setInterpolationMatrix(np.ones(12), 6)

@@ -1,0 +1,138 @@
+"""CPU oracle: analytic known answers, the reference's forcing semantics, a
+second (pure-Python) restatement, and finite differences for the adjoint."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from pasif_gb300.system import Pattern
+from tests import cases, refsem
+
+
+def oscillator(omega):
+    # x' = v, v' = -omega^2 x
+    pat, order = Pattern.from_dense_lists(2, [0, 1], [1, 0], f=[1])
+    v = np.array([1.0, -omega ** 2, 0.0])
+    return pat, v
+
+
+def test_linear_oscillator_closed_form_and_order():
+    omega, T = 1.3, 5.0
+    errs = []
+    for N in (500, 1000, 2000):
+        pat, v = oscillator(omega)
+        st, _, _ = O.batch_forward(pat, v[None], [[1.0, 0.0]], [0], np.zeros((1, 4)), T / N, N)
+        errs.append(abs(st[0, 0] - np.cos(omega * T)))
+    assert errs[0] < 1e-7
+    # classical RK4: global error O(h^4)
+    assert 12 < errs[0] / errs[1] < 20 and 12 < errs[1] / errs[2] < 20
+
+
+def test_zero_input_zero_output():
+    rng = np.random.default_rng(0)
+    pat, v = cases.random_system(rng, 4)
+    st, mx, sq = O.batch_forward(pat, v[None], np.zeros((1, 4)), [0], np.zeros((1, 50)), 1e-2, 40,
+                                 max_comp=[0], sq_comp=[1])
+    assert np.all(st == 0) and np.all(mx == 0) and np.all(sq == 0)
+
+
+def test_sample_and_hold_gating_known_answer():
+    # x' = u, u = 1 for every sample: sample 0 is never used, step s uses
+    # x[s] for k1..k3 and x[s+1] for k4 (src/kernels.cu:82-88), nothing past
+    # the end.  Over N = L steps: h/6 + (L-2) h + 5h/6 = (L-1) h.
+    pat, _ = Pattern.from_dense_lists(1, [], [], f=[0])
+    L, h = 37, 0.125
+    st, _, _ = O.batch_forward(pat, [[1.0]], [[0.0]], [0], np.ones((1, L)), h, L)
+    assert st[0, 0] == pytest.approx((L - 1) * h, rel=0, abs=1e-14)
+
+
+def test_interpolation_window_semantics():
+    # x' = u with W = 4 linear weights on a ramp x[j] = j: u(s2) = (s2 mod 4)/4
+    # between samples, zero while j == 0; compare with the Python restatement.
+    pat, _ = Pattern.from_dense_lists(1, [], [], f=[0])
+    W = 4
+    k = np.arange(W) / W
+    im = np.stack([k, 1 - k])
+    x = np.arange(30, dtype=float)[None]
+    h = 0.5
+    st, _, _ = O.batch_forward(pat, [[1.0]], [[0.0]], [0], x, h, 50, window=W, im=im)
+    ref = refsem.amplitudes(refsem.sysdict(pat, [1.0]), [0.0], refsem.excdict(x, W, im), h, 50)
+    assert st[0, 0] == pytest.approx(ref[0], rel=1e-14)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_matches_python_restatement(seed):
+    rng = np.random.default_rng(seed)
+    pat, v = cases.random_system(rng)
+    x0 = rng.normal(0, 0.3, pat.n)
+    E, L = 3, 40
+    x = cases.signals(rng, E, L)
+    W = [0, 2, 8][seed % 3]
+    im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
+    h, N = 0.05, 60   # runs past the end of the signals: exercises gating
+    got = O.get_amplitudes(pat, v, x0, x, h, N, W, im)
+    ref = refsem.amplitudes(refsem.sysdict(pat, v), x0, refsem.excdict(x, W, im), h, N)
+    np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-13)
+
+
+def test_float_oracle_tracks_double():
+    rng = np.random.default_rng(7)
+    pat, v = cases.random_system(rng, 5)
+    vals, x0 = cases.random_batch(rng, pat, v, 8)
+    x = cases.signals(rng, 2, 400)
+    e = np.arange(8) % 2
+    a, _, _ = O.batch_forward(pat, vals, x0, e, x, 0.01, 300, window=2, im=[[0, .5], [1, .5]])
+    b, _, _ = O.batch_forward(pat, vals, x0, e, x, 0.01, 300, window=2, im=[[0, .5], [1, .5]], precision="fp32_kahan")
+    np.testing.assert_allclose(b, a, rtol=1e-4, atol=1e-5)
+
+
+def test_gradient_ref_semantics_matches_python():
+    c = cases.one_dof_probe()
+    fpat, fo = Pattern.from_dense_lists(4, c["fk"][0], c["fk"][1], g=c["fg"][0], l=c["fl"][0], f=[2])
+    fv = np.concatenate([np.asarray(c["fk"][2])[fo], c["fg"][1], c["fl"][1], [1.0]])
+    bpat, bo = Pattern.from_dense_lists(6, c["bk"][0], c["bk"][1], l=c["bl"][0], p=c["bpsi"][0], n_sp=4)
+    bv = np.concatenate([np.asarray(c["bk"][2])[bo], c["bl"][1], c["bpsi"][1]])
+    rng = np.random.default_rng(3)
+    x = 1.0 + 0.1 * rng.standard_normal((2, 120))
+    for N in (50, 100, 117):   # lastC < C, lastC == C (100 = 10 * 10), ragged
+        got = O.get_gradient(fpat, fv, np.zeros(4), bpat, bv, c["a0"], x, 1 / 16, N)
+        ref = refsem.gradient(refsem.sysdict(fpat, fv), np.zeros(4), refsem.sysdict(bpat, bv), c["a0"],
+                              refsem.excdict(x), 1 / 16, N)
+        np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-13)
+
+
+def test_exact_adjoint_matches_finite_differences():
+    rng = np.random.default_rng(11)
+    pat, v = cases.random_system(rng, 4)
+    x0 = rng.normal(0, 0.3, 4)
+    x = cases.signals(rng, 1, 200)
+    h, N = 0.02, 150
+    gfin = rng.normal(size=4)
+    gsq = 0.7
+    sq = (0, 2)
+
+    def loss(vv, xx):
+        st, _, s = O.batch_forward(pat, vv[None], xx[None], [0], x, h, N, window=2, im=[[0, .5], [1, .5]],
+                                   sq_comp=sq, sq_start=N // 2)
+        return float(gfin @ st[0] + gsq * s[0])
+
+    dv, dx = O.batch_adjoint(pat, v[None], x0[None], [0], x, h, N, window=2, im=[[0, .5], [1, .5]],
+                             g_final=gfin[None], g_sq=[gsq], sq_comp=sq, sq_start=N // 2)
+    eps = 1e-6
+    fd = np.array([(loss(v + eps * e, x0) - loss(v - eps * e, x0)) / (2 * eps) for e in np.eye(v.size)])
+    np.testing.assert_allclose(dv[0], fd, rtol=2e-6, atol=1e-8)
+    fdx = np.array([(loss(v, x0 + eps * e) - loss(v, x0 - eps * e)) / (2 * eps) for e in np.eye(4)])
+    np.testing.assert_allclose(dx[0], fdx, rtol=2e-6, atol=1e-8)
+
+
+def test_trajectory_layout():
+    rng = np.random.default_rng(5)
+    pat, v = cases.random_system(rng, 3)
+    x0 = rng.normal(size=3)
+    x = cases.signals(rng, 2, 30)
+    N, save = 20, 3
+    tr = O.get_trajectory(pat, v, x0, x, 0.05, N, save)
+    assert tr.size == (3 * 2 * N) // save
+    # slot 1 = state after step 3 (t % 3 == 0 after step t = 3) for copy e
+    for e in range(2):
+        st = O.get_amplitudes(pat, v, x0, x[:, :], 0.05, 4)[e * 3:(e + 1) * 3]
+        np.testing.assert_array_equal(tr[(1 * 2 + e) * 3:(1 * 2 + e + 1) * 3], st)

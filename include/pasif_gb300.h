@@ -127,7 +127,8 @@ int pasif_driver_set_interpolation_matrix(pasif_driver* d, const double* matrix,
 int pasif_driver_set_modulation_buffer(pasif_driver* d, const double* buffer, long long n);
 
 /* _getAmplitudes (src/__GpuDriver.cu:416-461): final state of every
- * excitation copy, out[e * n + i].  out == NULL: only *out_len is set. */
+ * excitation copy, out[e * n + i].  For the three getters, out == NULL only
+ * sets *out_len (nothing is solved); otherwise capacity must hold it. */
 int pasif_driver_get_amplitudes(pasif_driver* d, double* out, long long capacity, long long* out_len);
 /* _getTrajectory (src/__GpuDriver.cu:463-500): the state after every step t
  * with t % save_steps == 0, laid out [slot][e][i], truncated to

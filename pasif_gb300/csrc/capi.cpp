@@ -232,9 +232,16 @@ int pasif_driver_set_modulation_buffer(pasif_driver* d, const double* buffer, lo
     return guard([&] { std::string err; return done(d->d->set_modulation(buffer, n, &err), err); });
 }
 
+// out == NULL: report the output size only, without solving (a solve may
+// change driver state: _getGradient chains the adjoint terminal condition).
 int pasif_driver_get_amplitudes(pasif_driver* d, double* out, long long capacity, long long* out_len) {
     DRV_CHECK(d);
     return guard([&] {
+        if (!out) {
+            if (out_len) *out_len = d->d->amplitudes_size();
+            return PASIF_OK;
+        }
+        if (capacity < d->d->amplitudes_size()) return fail(PASIF_ERR_INVALID, "output capacity too small");
         std::vector<double> v;
         std::string err;
         int rc = d->d->amplitudes(&v, &err);
@@ -247,6 +254,12 @@ int pasif_driver_get_trajectory(pasif_driver* d, unsigned save_steps, double* ou
                                 long long* out_len) {
     DRV_CHECK(d);
     return guard([&] {
+        if (save_steps == 0) return fail(PASIF_ERR_INVALID, "saveSteps must be positive");
+        if (!out) {
+            if (out_len) *out_len = d->d->trajectory_size(save_steps);
+            return PASIF_OK;
+        }
+        if (capacity < d->d->trajectory_size(save_steps)) return fail(PASIF_ERR_INVALID, "output capacity too small");
         std::vector<double> v;
         std::string err;
         int rc = d->d->trajectory(save_steps, &v, &err);
@@ -258,6 +271,11 @@ int pasif_driver_get_trajectory(pasif_driver* d, unsigned save_steps, double* ou
 int pasif_driver_get_gradient(pasif_driver* d, unsigned save, double* out, long long capacity, long long* out_len) {
     DRV_CHECK(d);
     return guard([&] {
+        if (!out) {
+            if (out_len) *out_len = d->d->gradient_size();
+            return PASIF_OK;
+        }
+        if (capacity < d->d->gradient_size()) return fail(PASIF_ERR_INVALID, "output capacity too small");
         std::vector<double> v;
         std::string err;
         int rc = d->d->gradient(save, &v, &err);

@@ -473,6 +473,15 @@ int Driver::gradient(unsigned save, std::vector<double>* out, std::string* err) 
                 for (int i = 0; i < na; ++i) a0[b * na + i] = bwd_state_[(size_t)e * na_ + bl.anodes[i]];
                 exc[b] = e;
             }
+        if (dsystem_) {
+            std::printf("[System] gradient group: %d blocks x %d signals, forward %s values", nb, E, b0.pat.key().c_str());
+            for (double v : b0.vals) std::printf(" %.17g", v);
+            std::printf("\n[System] adjoint %s values", b0.apat.key().c_str());
+            for (double v : b0.avals) std::printf(" %.17g", v);
+            std::printf("\n[System] a0");
+            for (double v : a0) std::printf(" %.17g", v);
+            std::printf("\n");
+        }
         rc = refgrad_run(*fp, *bp, B, fv.data(), bv.data(), x0.data(), a0.data(), exc.data(), *signals_, h_,
                          (int)numsteps_, (int)save, o.data(), stream_, err);
         if (rc) return rc;

@@ -67,6 +67,13 @@ public:
     int trajectory(unsigned save, std::vector<double>* out, std::string* err);
     int gradient(unsigned save, std::vector<double>* out, std::string* err);
     int last_kind() const { return last_kind_; }
+    // Output sizes of the getters (no solve): nf * n_exc, na * n_exc and
+    // floor(nf * n_exc * numsteps / save) (src/__GpuDriver.cu:420,469,580).
+    long long amplitudes_size() const { return (long long)nf_ * n_exc_; }
+    long long gradient_size() const { return (long long)na_ * n_exc_; }
+    long long trajectory_size(unsigned save) const {
+        return save ? ((long long)nf_ * n_exc_ * (long long)numsteps_) / (long long)save : 0;
+    }
 
 private:
     int ensure_signals(std::string* err);

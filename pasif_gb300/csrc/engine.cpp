@@ -350,6 +350,9 @@ int Batch::get(double* state_out, double* max_out, double* sq_out, double h, int
     if (sq_out && has_sq) {
         rc = download_interleaved(out_sq.p, B, 1, f, h, sq_out, memory, stage, st, err);
         if (rc) return rc;
+    } else if (sq_out && B > 0) {   // no sum-of-squares reducer: defined as 0
+        if (memory == kHost) std::memset(sq_out, 0, sizeof(double) * B);
+        else PK_CUDA(cudaMemsetAsync(sq_out, 0, sizeof(double) * B, st), "cudaMemsetAsync");
     }
     PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     return 0;

@@ -221,6 +221,23 @@ int pasif_forward(const pasif_pattern* pattern, int precision, int n_sys, const 
                   int window, const double* im, double h, int step0, int nsteps,
                   const pasif_reducers* red, double* state, double* max, double* sq);
 
+/* Forward solve for callers that cannot allocate device memory (code inside
+ * another framework's memory pool or under a fixed memory budget, code that
+ * must not trigger the device synchronisation cudaMalloc/cudaFree can cause,
+ * applications that reserve all memory up front).  No counterpart in the
+ * reference.  FP64, final state only.  Every array except the pattern is a
+ * DEVICE pointer: values[n_sys][P], x0[n_sys][n], exc_index[n_sys],
+ * signals[n_exc][len], im[2*window] (window 0: sample and hold),
+ * state_out[n_sys][n].  Work space: a 32 MiB array owned by the library on
+ * every GPU that loads it (until exit); 8*n_sys*(P+7n) bytes must fit in
+ * 31 MiB and the pattern in 1 MiB, else PASIF_ERR_INVALID.  The first call on
+ * a device looks up the array's address (make it before any stream
+ * capture).  Calls share the array and keep its last contents: calls whose
+ * GPU work overlaps race.  Returns once the work is queued on `stream`. */
+int pasif_forward_noalloc(const pasif_pattern* pattern, int n_sys, const double* values, const double* x0,
+                          const int* exc_index, const double* signals, int n_exc, int len, int window,
+                          const double* im, double h, int step0, int nsteps, double* state_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

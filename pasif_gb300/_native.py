@@ -110,6 +110,8 @@ _SIGS = {
     "pasif_plan_jit_report": (C.c_int, [_vp, _dp, C.c_int, C.c_ulonglong, C.c_ulonglong, C.c_char_p,
                                         C.c_longlong, _llp]),
     "pasif_fma_peak": (C.c_int, [C.c_int, _dp]),
+    "pasif_forward_noalloc": (C.c_int, [C.POINTER(PatternC), C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int,
+                                        _vp, C.c_double, C.c_int, C.c_int, _vp, _vp]),
     "pasif_forward": (C.c_int, [C.POINTER(PatternC), C.c_int, C.c_int, _dp, _dp, _ip, _dp, C.c_int, C.c_int,
                                 C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.POINTER(ReducersC), _dp, _dp, _dp]),
 }

@@ -21,7 +21,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["generic_kernels.cu"]
+CU_SOURCES = ["generic_kernels.cu", "noalloc.cu"]
 CPP_SOURCES = ["engine.cpp", "jit.cpp", "driver.cpp", "capi.cpp", "pattern.cpp"]
 EMBEDDED = ["pk_args.h", "rk4_core.cuh"]
 

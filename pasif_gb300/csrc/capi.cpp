@@ -100,6 +100,8 @@ int copy_out(const std::vector<double>& v, double* out, long long cap, long long
 
 }  // namespace
 
+void pasif_internal_set_error(const std::string& msg) { g_err = msg; }
+
 extern "C" {
 
 const char* pasif_last_error(void) { return g_err.c_str(); }

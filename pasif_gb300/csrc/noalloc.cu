@@ -1,0 +1,177 @@
+// noalloc.cu -- a forward solve that allocates no device memory.
+//
+// Some callers cannot call cudaMalloc: code that runs inside another
+// framework's memory pool or under a strict memory budget, code that must not
+// synchronise the device (cudaMalloc/cudaFree may), and applications that
+// reserve all device memory up front and hand out slices of it.  For them,
+// pasif_forward_noalloc runs the generic (pattern-interpreting) FP64 forward
+// kernel with its work space -- the pattern, the instance values and state in
+// the kernel's [k][n_sys] layout, and the kernel's per-instance work vectors
+// -- in one fixed-size array that lives in the library's own device memory
+// (a file-scope __device__ array).  The caller passes inputs and outputs in
+// device memory; nothing is allocated, on the device or on the host heap.
+//
+// Limits and rules:
+//   * the array holds kNoallocBytes = 32 MiB on every GPU that loads the
+//     library, for as long as the process lives; the first 1 MiB holds the
+//     pattern (<= 262144 integers), the rest 8 * n_sys * (P + 7 n) bytes;
+//     larger requests are rejected with PASIF_ERR_INVALID;
+//   * the first call on a device looks up the array's device address with
+//     cudaGetSymbolAddress (a host-side name is not a device address); make
+//     that first call before any stream capture;
+//   * every call shares the one array and leaves its last contents there:
+//     calls whose GPU work overlaps (different streams, threads) race.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/pasif_gb300.h"
+#include "generic_kernels.h"
+#include "pk_args.h"
+
+// Sets the thread-local message returned by pasif_last_error (capi.cpp).
+void pasif_internal_set_error(const std::string& msg);
+
+namespace {
+
+constexpr size_t kNoallocBytes = 32u << 20;
+constexpr size_t kPatternBytes = 1u << 20;
+constexpr int kMaxDevices = 64;
+
+__device__ __align__(256) unsigned char pk_noalloc_scratch[kNoallocBytes];
+
+std::mutex g_mu;
+void* g_addr[kMaxDevices] = {};
+
+// Device address of pk_noalloc_scratch on the current device (set-up once
+// per device).
+cudaError_t scratch_address(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, pk_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_addr[dev] = p;
+    }
+    *out = g_addr[dev];
+    return cudaSuccess;
+}
+
+int fail(int code, const std::string& msg) {
+    pasif_internal_set_error(msg);
+    return code;
+}
+
+bool pow2(int w) { return w > 0 && !(w & (w - 1)); }
+
+}  // namespace
+
+extern "C" int pasif_forward_noalloc(const pasif_pattern* pat, int n_sys, const double* values, const double* x0,
+                                     const int* exc_index, const double* signals, int n_exc, int len, int window,
+                                     const double* im, double h, int step0, int nsteps, double* state_out,
+                                     void* stream) {
+    if (!pat || pat->n < 0 || pat->k_nnz < 0 || pat->g_nnz < 0 || pat->l_nnz < 0 || pat->p_nnz < 0 ||
+        pat->f_nnz < 0 || !pat->k_ptr)
+        return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: bad pattern");
+    const int n = pat->n;
+    const long long P = (long long)pat->k_nnz + pat->g_nnz + pat->l_nnz + pat->p_nnz + pat->f_nnz;
+    const long long pat_ints = (n + 1LL) + pat->k_nnz + 3LL * pat->g_nnz + 4LL * pat->l_nnz + 5LL * pat->p_nnz +
+                               pat->f_nnz;
+    if (n_sys < 0 || nsteps < 0 || step0 < 0) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: negative size");
+    if (n_exc < 1 || len < 1 || !signals) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: empty signal table");
+    if (window < 0 || (window > 0 && (!pow2(window) || !im)))
+        return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: window must be 0 or a power of two with weights");
+    if (!(h > 0.0) || !std::isfinite(h)) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: bad time step");
+    if ((size_t)pat_ints * sizeof(int) > kPatternBytes)
+        return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: pattern larger than the 1 MiB pattern area");
+    const double need = 8.0 * (double)n_sys * (double)(P + 7LL * n);
+    if (need > (double)(kNoallocBytes - kPatternBytes))
+        return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: 8*n_sys*(P+7n) = " + std::to_string((long long)need) +
+                                           " bytes exceeds the 31 MiB static work space; split the batch");
+    if (n_sys == 0) return PASIF_OK;
+    if (!x0 || !exc_index || !state_out || (P > 0 && !values))
+        return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: null input or output");
+    // pattern checks (host arrays)
+    for (int i = 0; i < n; ++i)
+        if (pat->k_ptr[i + 1] < pat->k_ptr[i]) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: bad CSR");
+    if (pat->k_ptr[0] != 0 || pat->k_ptr[n] != pat->k_nnz) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: bad CSR");
+    for (int q = 0; q < pat->k_nnz; ++q)
+        if (pat->k_col[q] < 0 || pat->k_col[q] >= n) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: bad index");
+    const int* lists[4] = {pat->g_idx, pat->l_idx, pat->p_idx, pat->f_idx};
+    const long long counts[4] = {3LL * pat->g_nnz, 4LL * pat->l_nnz, 5LL * pat->p_nnz, pat->f_nnz};
+    for (int l = 0; l < 4; ++l)
+        for (long long q = 0; q < counts[l]; ++q)
+            if (lists[l][q] < 0 || lists[l][q] >= n) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: bad index");
+    cudaStream_t st = (cudaStream_t)stream;
+    // excitation indices are device data: checked in fixed-size host chunks
+    {
+        int chunk[1024];
+        for (int b0 = 0; b0 < n_sys; b0 += 1024) {
+            const int m = n_sys - b0 < 1024 ? n_sys - b0 : 1024;
+            cudaError_t e = cudaMemcpyAsync(chunk, exc_index + b0, sizeof(int) * m, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return fail(PASIF_ERR_CUDA, std::string("pasif_forward_noalloc: ") + cudaGetErrorString(e));
+            for (int i = 0; i < m; ++i)
+                if (chunk[i] < 0 || chunk[i] >= n_exc)
+                    return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: excitation index out of range");
+        }
+    }
+    void* base = nullptr;
+    cudaError_t e = scratch_address(&base);
+    if (e != cudaSuccess) return fail(PASIF_ERR_CUDA, std::string("pasif_forward_noalloc: symbol address: ") + cudaGetErrorString(e));
+    int* d_pat = static_cast<int*>(base);
+    double* d_vals = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + kPatternBytes);
+    double* d_state = d_vals + (size_t)P * n_sys;
+    double* d_work = d_state + (size_t)n * n_sys;
+    // pattern: k_ptr | k_col | g | l | p | f (the generic kernels' layout)
+    const int* parts[6] = {pat->k_ptr, pat->k_col, pat->g_idx, pat->l_idx, pat->p_idx, pat->f_idx};
+    const long long sizes[6] = {n + 1LL, pat->k_nnz, 3LL * pat->g_nnz, 4LL * pat->l_nnz, 5LL * pat->p_nnz, pat->f_nnz};
+    long long off = 0;
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
+        if (sizes[k] > 0) e = cudaMemcpyAsync(d_pat + off, parts[k], sizeof(int) * sizes[k], cudaMemcpyHostToDevice, st);
+        off += sizes[k];
+    }
+    if (e == cudaSuccess) e = pk::launch_to_interleaved(values, d_vals, n_sys, (int)P, false, st);
+    if (e == cudaSuccess) e = pk::launch_to_interleaved(x0, d_state, n_sys, n, false, st);
+    if (e != cudaSuccess) return fail(PASIF_ERR_CUDA, std::string("pasif_forward_noalloc: ") + cudaGetErrorString(e));
+    pk::FwdArgs<double> a;
+    memset(&a, 0, sizeof(a));
+    a.vals = d_vals;
+    a.state = d_state;
+    a.exc_index = exc_index;
+    a.scratch = d_work;
+    a.traj_every = 1;
+    a.frc.x = signals;
+    a.frc.im = window ? im : nullptr;
+    a.frc.total = (long long)n_exc * len;
+    a.frc.len = (unsigned)len;
+    a.frc.w = (unsigned)window;
+    a.frc.lw = 0;
+    while (window > 0 && (1u << a.frc.lw) < (unsigned)window) a.frc.lw++;
+    a.gp.data = d_pat;
+    a.gp.n = n;
+    a.gp.n_sp = pat->n_sp > 0 ? pat->n_sp : n;
+    a.gp.k_nnz = pat->k_nnz;
+    a.gp.g_nnz = pat->g_nnz;
+    a.gp.l_nnz = pat->l_nnz;
+    a.gp.p_nnz = pat->p_nnz;
+    a.gp.f_nnz = pat->f_nnz;
+    a.gp.P = (int)P;
+    a.h = h;
+    a.h2 = h / 2.0;
+    a.h6 = h / 6.0;
+    a.B = n_sys;
+    a.step0 = (unsigned)step0;
+    a.nsteps = nsteps;
+    e = pk::launch_gen_fwd(a, false, st);
+    if (e == cudaSuccess) e = pk::launch_from_interleaved(d_state, state_out, n_sys, n, false, st, 1.0);
+    if (e != cudaSuccess) return fail(PASIF_ERR_CUDA, std::string("pasif_forward_noalloc: ") + cudaGetErrorString(e));
+    return PASIF_OK;
+}

@@ -204,10 +204,13 @@ int pasif_batch_kernel_info(pasif_batch* b, int* kind, int* registers);
 
 /* Compile (without loading; no GPU needed) the pattern-specialised forward
  * kernel that pasif_batch_forward would use for these host values, and copy
- * the compiler's resource report (registers, spills) into log.  kahan / the
- * reducer masks select the variant.  Diagnostic; no reference counterpart. */
+ * the compiler's resource report (registers, spills) into log, followed by
+ * the generated source after a line "// ---- source ----".  The reducer
+ * masks and the forcing window / weights (im[2*window]) select the variant.
+ * Diagnostic; no reference counterpart. */
 int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys,
                           unsigned long long max_mask, unsigned long long sq_mask,
+                          int window, const double* im,
                           char* log, long long capacity, long long* out_len);
 
 /* Measured FMA-pipe throughput of the current GPU in FLOP/s (FMA = 2 FLOP),

@@ -22,10 +22,12 @@
  * The reference sums the nonlinear terms with atomicAdd, so its FP order is
  * not fixed.  The oracle fixes one canonical order, which the CUDA kernels of
  * pasif_gb300 follow term for term:
- *   for every destination i: the CSR row of K in stored order, then the Gamma
- *   entries with dest i in COO order, then Lambda, then Psi, then the force
- *   entries; every term is folded with one fma:  acc = fma(term_without_last_factor,
- *   last_factor, acc), starting from acc = +0.
+ *   for every destination i, the terms in the order [CSR row of K | Gamma
+ *   entries with dest i in COO order | Lambda | Psi | force entries] are dealt
+ *   in turn to two partial sums (term k to sum k mod 2); a partial sum starts
+ *   as the product of its first term, acc = term_without_last_factor *
+ *   last_factor, and folds every further term with one fma; f[i] = sum0 +
+ *   sum1 when i has two or more terms, sum0 with one, +0 with none.
  * Every function exists in double (suffix _d) and float (suffix _f); the float
  * versions round every input once to float and compute in float.
  */

@@ -38,16 +38,18 @@ class Plan:
                                         N.PLAN_GENERIC_ONLY if generic_only else 0))
         self.handle = h
 
-    def jit_report(self, values=None, max_mask: int = 0, sq_mask: int = 0) -> str:
-        """Compiler resource report of the specialised forward kernel (no GPU needed)."""
+    def jit_report(self, values=None, max_mask: int = 0, sq_mask: int = 0, window: int = 0, im=None) -> str:
+        """Compiler resource report of the specialised forward kernel, then its
+        source after "// ---- source ----" (NVRTC only: no GPU needed)."""
         v = N.f64(values) if values is not None else None
         n_sys = int(v.shape[0]) if v is not None else 0
+        w = N.f64(im).reshape(-1) if im is not None else None
+        args = (self.handle, N.dptr(v) if v is not None else None, n_sys, max_mask, sq_mask, int(window),
+                N.dptr(w) if w is not None else None)
         ln = C.c_longlong()
-        N.check(N.lib.pasif_plan_jit_report(self.handle, N.dptr(v) if v is not None else None, n_sys, max_mask,
-                                            sq_mask, None, 0, C.byref(ln)))
+        N.check(N.lib.pasif_plan_jit_report(*args, None, 0, C.byref(ln)))
         buf = C.create_string_buffer(ln.value + 1)
-        N.check(N.lib.pasif_plan_jit_report(self.handle, N.dptr(v) if v is not None else None, n_sys, max_mask,
-                                            sq_mask, buf, ln.value + 1, C.byref(ln)))
+        N.check(N.lib.pasif_plan_jit_report(*args, buf, ln.value + 1, C.byref(ln)))
         return buf.value.decode()
 
     def __del__(self):

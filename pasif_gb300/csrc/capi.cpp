@@ -406,7 +406,8 @@ int pasif_fma_peak(int precision, double* flops_per_second) {
 }
 
 int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys, unsigned long long max_mask,
-                          unsigned long long sq_mask, char* log, long long capacity, long long* out_len) {
+                          unsigned long long sq_mask, int window, const double* im, char* log, long long capacity,
+                          long long* out_len) {
     if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null plan");
     return guard([&] {
         const pasif::Pattern& pat = p->p->pat;
@@ -431,8 +432,16 @@ int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys, 
         key.kahan = p->p->precision == pasif::kFP32Kahan;
         key.max_mask = max_mask;
         key.sq_mask = sq_mask;
+        if (window < 0 || (window > 0 && (!im || (window & (window - 1)))))
+            return fail(PASIF_ERR_INVALID, "window must be 0 or a power of two with weights");
+        key.window = window;
+        for (int i = 0; i < 2 * window; ++i) {
+            const double w = f32 ? (double)(float)im[i] : im[i];
+            (i < window ? key.wn : key.wc).push_back(w);
+        }
         std::string report, err;
         if (!pasif::fwd_compile_report(pat, lit, key, &report, &err)) return fail(PASIF_ERR_NVRTC, err);
+        report += "\n// ---- source ----\n" + pasif::fwd_source(pat, lit, key);
         if (out_len) *out_len = (long long)report.size();
         if (log && capacity > 0) {
             const size_t n = std::min<size_t>(report.size(), (size_t)capacity - 1);

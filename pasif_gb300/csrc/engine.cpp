@@ -124,6 +124,12 @@ int signals_create(const double* x, int n_exc, int len, int window, const double
     if (window > 0) {
         rc = upload_conv(im, 2LL * window, s->f32, memory, s->im, stage, st, err);
         if (rc) return rc;
+        // host copy of the weights (baked into specialised kernels)
+        std::vector<double> w(2 * (size_t)window);
+        if (memory == kHost) std::memcpy(w.data(), im, sizeof(double) * w.size());
+        else PK_CUDA(cudaMemcpy(w.data(), im, sizeof(double) * w.size(), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        for (double& v : w) v = s->f32 ? (double)(float)v : v;
+        s->im_host = w;
     }
     PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     *out = s;
@@ -298,6 +304,9 @@ int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Re
         key.sq_mask = sm;
         key.traj = traj_every > 0;
         key.block = 128;
+        key.window = (int)sig.w;
+        key.wn.assign(sig.im_host.begin(), sig.im_host.begin() + sig.w);
+        key.wc.assign(sig.im_host.begin() + sig.w, sig.im_host.end());
         JitKernel k;
         std::string jerr;
         if (get_fwd_kernel(pat, lit, key, &k, &jerr)) {

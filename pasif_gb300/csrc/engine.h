@@ -38,6 +38,7 @@ struct Signals {
     int len = 0;
     unsigned w = 0, lw = 0;
     DevBuf x, im;
+    std::vector<double> im_host;   // the 2W weights rounded to the compute precision
     template <typename R> pk::Forcing<R> forcing() const {
         pk::Forcing<R> f;
         f.x = x.as<R>();

@@ -49,37 +49,51 @@ struct Emitter {
         return hexlit(lit.value[q]);
     }
 
-    // rhs body: per destination, K row, Gamma, Lambda, Psi, forcing.
-    void rhs(std::ostringstream& o) const {
+    // rhs body.  Per destination, the terms [K row | Gamma | Lambda | Psi |
+    // forcing] are dealt in turn to two partial sums (a, c), each fma-folded
+    // from +0, and added when both are used: the canonical order of the
+    // oracle and of GenSys::rhs.  `force` selects the FORCE=true body.
+    void rhs(std::ostringstream& o, bool force) const {
         const int n = pat.n;
         const int go = pat.k_nnz(), lo = go + pat.g_nnz(), po = lo + pat.l_nnz(), fo = po + pat.p_nnz();
-        std::vector<std::vector<std::string>> terms(n);
+        // each term as (first factor expression, last factor expression)
+        std::vector<std::vector<std::pair<std::string, std::string>>> terms(n);
         for (int i = 0; i < n; ++i)
             for (int q = pat.k_ptr[i]; q < pat.k_ptr[i + 1]; ++q)
-                terms[i].push_back("a = m::fma(" + val(q) + ", xs[" + std::to_string(pat.k_col[q]) + "], a);");
+                terms[i].push_back({val(q), "xs[" + std::to_string(pat.k_col[q]) + "]"});
         for (int e = 0; e < pat.g_nnz(); ++e) {
             const int* ix = &pat.g_idx[3 * e];
-            terms[ix[0]].push_back("a = m::fma(m::mul(" + val(go + e) + ", xs[" + std::to_string(ix[1]) +
-                                   "]), xp[" + std::to_string(ix[2]) + "], a);");
+            terms[ix[0]].push_back({"m::mul(" + val(go + e) + ", xs[" + std::to_string(ix[1]) + "])",
+                                    "xp[" + std::to_string(ix[2]) + "]"});
         }
         for (int e = 0; e < pat.l_nnz(); ++e) {
             const int* ix = &pat.l_idx[4 * e];
-            terms[ix[0]].push_back("a = m::fma(m::mul(m::mul(" + val(lo + e) + ", xs[" + std::to_string(ix[1]) +
-                                   "]), xp[" + std::to_string(ix[2]) + "]), xp[" + std::to_string(ix[3]) +
-                                   "], a);");
+            terms[ix[0]].push_back({"m::mul(m::mul(" + val(lo + e) + ", xs[" + std::to_string(ix[1]) + "]), xp[" +
+                                        std::to_string(ix[2]) + "])",
+                                    "xp[" + std::to_string(ix[3]) + "]"});
         }
         for (int e = 0; e < pat.p_nnz(); ++e) {
             const int* ix = &pat.p_idx[5 * e];
-            terms[ix[0]].push_back("a = m::fma(m::mul(m::mul(m::mul(" + val(po + e) + ", xs[" +
-                                   std::to_string(ix[1]) + "]), xp[" + std::to_string(ix[2]) + "]), xp[" +
-                                   std::to_string(ix[3]) + "]), xp[" + std::to_string(ix[4]) + "], a);");
+            terms[ix[0]].push_back({"m::mul(m::mul(m::mul(" + val(po + e) + ", xs[" + std::to_string(ix[1]) +
+                                        "]), xp[" + std::to_string(ix[2]) + "]), xp[" + std::to_string(ix[3]) + "])",
+                                    "xp[" + std::to_string(ix[4]) + "]"});
         }
-        for (int e = 0; e < pat.f_nnz(); ++e)
-            terms[pat.f_idx[e]].push_back("if (FORCE) a = m::fma(" + val(fo + e) + ", u, a);");
+        if (force)
+            for (int e = 0; e < pat.f_nnz(); ++e) terms[pat.f_idx[e]].push_back({val(fo + e), "u"});
         for (int i = 0; i < n; ++i) {
-            o << "    a = R(0);\n";
-            for (auto& t : terms[i]) o << "    " << t << "\n";
-            o << "    f[" << i << "] = a;\n";
+            if (terms[i].empty()) {
+                o << "      f[" << i << "] = R(0);\n";
+                continue;
+            }
+            for (size_t k = 0; k < terms[i].size(); ++k) {
+                const char* acc = (k & 1) ? "c" : "a";
+                if (k < 2)
+                    o << "      " << acc << " = m::mul(" << terms[i][k].first << ", " << terms[i][k].second << ");\n";
+                else
+                    o << "      " << acc << " = m::fma(" << terms[i][k].first << ", " << terms[i][k].second << ", "
+                      << acc << ");\n";
+            }
+            o << "      f[" << i << "] = " << (terms[i].size() >= 2 ? "m::add(a, c)" : "a") << ";\n";
         }
     }
 };
@@ -112,6 +126,7 @@ bool to_cubin(const std::string& src, std::vector<char>* cubin, std::string* log
     nvrtcGetProgramLogSize(prog, &ls);
     std::string text(ls, '\0');
     if (ls) nvrtcGetProgramLog(prog, &text[0]);
+    while (!text.empty() && text.back() == '\0') text.pop_back();
     if (rc != NVRTC_SUCCESS) {
         *err = std::string("NVRTC compile failed: ") + nvrtcGetErrorString(rc) + "\n" + text;
         nvrtcDestroyProgram(&prog);
@@ -163,18 +178,32 @@ std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelK
     o << "  }\n";
     o << "  template <bool FORCE, class V, class W, class F>\n";
     o << "  __device__ __forceinline__ void rhs(const V& xs, const W& xp, R u, F& f) const {\n";
-    o << "    typedef M<R> m;\n    R a;\n";
-    em.rhs(o);
-    o << "  }\n};\n}  // namespace pk\n";
+    o << "    typedef M<R> m;\n    R a, c;\n";
+    o << "    if (FORCE) {\n";
+    em.rhs(o, true);
+    o << "    } else {\n";
+    em.rhs(o, false);
+    o << "    }\n";
+    o << "  }\n};\n";
+    // forcing window and weights as compile-time constants
+    const int W = key.window;
+    o << "struct JW {\n  static constexpr int W = " << W << ";\n";
+    for (int which = 0; which < 2; ++which) {
+        o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";
+        const std::vector<double>& wv = which ? key.wc : key.wn;
+        for (int i = 0; i < W; ++i) o << "i == " << i << " ? " << hexlit(wv[i]) << " : ";
+        o << "R(0); }\n";
+    }
+    o << "};\n}  // namespace pk\n";
     o << "extern \"C\" __global__ void __launch_bounds__(" << key.block << ") pk_fwd(pk::FwdArgs<pk::R> a) {\n";
     o << "  using namespace pk;\n";
     o << "  const int b = blockIdx.x * blockDim.x + threadIdx.x;\n";
     o << "  if (b >= a.B) return;\n";
     o << "  JSys sys;\n  sys.load(a.vals, (long long)a.B, b);\n";
     o << "  RegVec<R, " << n << "> Q, Cm, S, K, Mi, Mx;\n";
-    o << "  fwd_run<R, " << n << ", " << (key.kahan ? "true" : "false") << ", "
+    o << "  fwd_run_iv<R, " << n << ", " << (key.kahan ? "true" : "false") << ", "
       << (key.max_mask ? "true" : "false") << ", " << (key.sq_mask ? "true" : "false") << ", "
-      << (key.traj ? "true" : "false") << ">(sys, a, b, "
+      << (key.traj ? "true" : "false") << ", JW>(sys, a, b, "
       << key.max_mask << "ull, " << key.sq_mask << "ull, Q, Cm, S, K, Mi, Mx);\n";
     o << "}\n";
     return o.str();

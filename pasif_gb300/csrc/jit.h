@@ -24,6 +24,8 @@ struct FwdKernelKey {
     unsigned long long sq_mask = 0;
     bool traj = false;
     int block = 128;
+    int window = 0;                 // forcing window (0 = sample and hold)
+    std::vector<double> wn, wc;     // its weights in the compute precision
 };
 
 struct JitKernel {

@@ -71,6 +71,40 @@ int fail(int code, const std::string& msg) {
 
 bool pow2(int w) { return w > 0 && !(w & (w - 1)); }
 
+// Appends to the flat pattern the per-destination term lists the generic
+// kernels read (d_ptr[n+1] | term[P], same encoding as Pattern::flat) by a
+// counting sort: count per destination, prefix sum, then place the terms in
+// parameter order (K, Gamma, Lambda, Psi, F), which keeps every list in
+// canonical order.  One thread, O(n + P); cur[n] follows the term list.
+__global__ void build_term_lists(int* d, int n, int kn, int gn, int ln, int pn, int fn) {
+    const int* kp = d;
+    const int* gi = d + (n + 1) + kn;
+    const int* li = gi + 3 * gn;
+    const int* pi = li + 4 * ln;
+    const int* fi = pi + 5 * pn;
+    int* dp = d + (n + 1) + kn + 3 * gn + 4 * ln + 5 * pn + fn;
+    int* tl = dp + n + 1;
+    int* cur = tl + kn + gn + ln + pn + fn;
+    for (int i = 0; i <= n; ++i) dp[i] = 0;
+    for (int i = 0; i < n; ++i) dp[i + 1] += kp[i + 1] - kp[i];
+    for (int e = 0; e < gn; ++e) dp[gi[3 * e] + 1]++;
+    for (int e = 0; e < ln; ++e) dp[li[4 * e] + 1]++;
+    for (int e = 0; e < pn; ++e) dp[pi[5 * e] + 1]++;
+    for (int e = 0; e < fn; ++e) dp[fi[e] + 1]++;
+    for (int i = 0; i < n; ++i) dp[i + 1] += dp[i];
+    for (int i = 0; i < n; ++i) cur[i] = dp[i];
+    for (int i = 0; i < n; ++i)
+        for (int q = kp[i]; q < kp[i + 1]; ++q) tl[cur[i]++] = q;
+    int base = kn;
+    for (int e = 0; e < gn; ++e) tl[cur[gi[3 * e]]++] = (1 << 28) | (base + e);
+    base += gn;
+    for (int e = 0; e < ln; ++e) tl[cur[li[4 * e]]++] = (2 << 28) | (base + e);
+    base += ln;
+    for (int e = 0; e < pn; ++e) tl[cur[pi[5 * e]]++] = (3 << 28) | (base + e);
+    base += pn;
+    for (int e = 0; e < fn; ++e) tl[cur[fi[e]]++] = (4 << 28) | (base + e);
+}
+
 }  // namespace
 
 extern "C" int pasif_forward_noalloc(const pasif_pattern* pat, int n_sys, const double* values, const double* x0,
@@ -83,7 +117,7 @@ extern "C" int pasif_forward_noalloc(const pasif_pattern* pat, int n_sys, const 
     const int n = pat->n;
     const long long P = (long long)pat->k_nnz + pat->g_nnz + pat->l_nnz + pat->p_nnz + pat->f_nnz;
     const long long pat_ints = (n + 1LL) + pat->k_nnz + 3LL * pat->g_nnz + 4LL * pat->l_nnz + 5LL * pat->p_nnz +
-                               pat->f_nnz;
+                               pat->f_nnz + (n + 1LL) + P + n;   // + term lists and their cursors
     if (n_sys < 0 || nsteps < 0 || step0 < 0) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: negative size");
     if (n_exc < 1 || len < 1 || !signals) return fail(PASIF_ERR_INVALID, "pasif_forward_noalloc: empty signal table");
     if (window < 0 || (window > 0 && (!pow2(window) || !im)))
@@ -137,6 +171,11 @@ extern "C" int pasif_forward_noalloc(const pasif_pattern* pat, int n_sys, const 
     for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
         if (sizes[k] > 0) e = cudaMemcpyAsync(d_pat + off, parts[k], sizeof(int) * sizes[k], cudaMemcpyHostToDevice, st);
         off += sizes[k];
+    }
+    // per-destination term lists (d_ptr | terms) built on the device
+    if (e == cudaSuccess) {
+        build_term_lists<<<1, 1, 0, st>>>(d_pat, n, pat->k_nnz, pat->g_nnz, pat->l_nnz, pat->p_nnz, pat->f_nnz);
+        e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = pk::launch_to_interleaved(values, d_vals, n_sys, (int)P, false, st);
     if (e == cudaSuccess) e = pk::launch_to_interleaved(x0, d_state, n_sys, n, false, st);

@@ -42,7 +42,24 @@ std::vector<int> Pattern::flat() const {
     v.insert(v.end(), l_idx.begin(), l_idx.end());
     v.insert(v.end(), p_idx.begin(), p_idx.end());
     v.insert(v.end(), f_idx.begin(), f_idx.end());
-    if (v.empty()) v.push_back(0);
+    // per-destination term lists in canonical order: d_ptr[n+1] | term[P],
+    // term = (kind << 28) | parameter index, kind 0 K, 1 Gamma, 2 Lambda,
+    // 3 Psi, 4 F (forcing terms last in each list)
+    std::vector<std::vector<int>> per(n);
+    const int go = k_nnz(), lo = go + g_nnz(), po = lo + l_nnz(), fo = po + p_nnz();
+    for (int i = 0; i < n; ++i)
+        for (int q = k_ptr[i]; q < k_ptr[i + 1]; ++q) per[i].push_back(q);
+    for (int e = 0; e < g_nnz(); ++e) per[g_idx[3 * e]].push_back((1 << 28) | (go + e));
+    for (int e = 0; e < l_nnz(); ++e) per[l_idx[4 * e]].push_back((2 << 28) | (lo + e));
+    for (int e = 0; e < p_nnz(); ++e) per[p_idx[5 * e]].push_back((3 << 28) | (po + e));
+    for (int e = 0; e < f_nnz(); ++e) per[f_idx[e]].push_back((4 << 28) | (fo + e));
+    int acc = 0;
+    v.push_back(0);
+    for (int i = 0; i < n; ++i) {
+        acc += (int)per[i].size();
+        v.push_back(acc);
+    }
+    for (int i = 0; i < n; ++i) v.insert(v.end(), per[i].begin(), per[i].end());
     return v;
 }
 

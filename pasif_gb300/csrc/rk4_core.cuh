@@ -92,6 +92,11 @@ struct GenSys {
     __device__ __forceinline__ R val(int p) const { return vals[(long long)p * B + b]; }
 
     // f = K.xs + Gamma:(xs,xp) + Lambda:(xs,xp,xp) + Psi:(xs,xp,xp,xp) [+ F u]
+    // Canonical accumulation: the terms of destination i (K row, Gamma,
+    // Lambda, Psi, F; the per-destination lists built by Pattern::flat) are
+    // dealt in turn to two partial sums, each starting as the product of its
+    // first term and folding the others with one fma; f[i] is their sum when
+    // i has two or more terms, the first with one, +0 with none.
     template <bool FORCE, class V, class W, class F>
     __device__ __noinline__ void rhs(const V& xs, const W& xp, R u, F& f) const {
         typedef M<R> m;
@@ -101,31 +106,49 @@ struct GenSys {
         const int* li = gi + 3 * g.g_nnz;
         const int* pi = li + 4 * g.l_nnz;
         const int* fi = pi + 5 * g.p_nnz;
+        const int* dp = fi + g.f_nnz;
+        const int* tl = dp + g.n + 1;
+        const int go = g.k_nnz, lo = go + g.g_nnz, po = lo + g.l_nnz, fo = po + g.p_nnz;
         for (int i = 0; i < g.n; ++i) {
-            R acc = R(0);
-            for (int p = kp[i]; p < kp[i + 1]; ++p) acc = m::fma(val(p), xs[kc[p]], acc);
-            f[i] = acc;
+            R a0 = R(0), a1 = R(0);
+            int k = 0;
+            for (int t = dp[i]; t < dp[i + 1]; ++t) {
+                const int code = tl[t];
+                const int kind = code >> 28, q = code & 0x0fffffff;
+                R x, y;
+                if (kind == 0) {
+                    x = val(q);
+                    y = xs[kc[q]];
+                } else if (kind == 1) {
+                    const int* ix = gi + 3 * (q - go);
+                    x = m::mul(val(q), xs[ix[1]]);
+                    y = xp[ix[2]];
+                } else if (kind == 2) {
+                    const int* ix = li + 4 * (q - lo);
+                    x = m::mul(m::mul(val(q), xs[ix[1]]), xp[ix[2]]);
+                    y = xp[ix[3]];
+                } else if (kind == 3) {
+                    const int* ix = pi + 5 * (q - po);
+                    x = m::mul(m::mul(m::mul(val(q), xs[ix[1]]), xp[ix[2]]), xp[ix[3]]);
+                    y = xp[ix[4]];
+                } else {
+                    if (!FORCE) break;   // forcing terms close every list
+                    x = val(q);
+                    y = u;
+                    (void)fo;
+                }
+                if (k < 2) {
+                    if (k) a1 = m::mul(x, y);
+                    else a0 = m::mul(x, y);
+                } else if (k & 1) {
+                    a1 = m::fma(x, y, a1);
+                } else {
+                    a0 = m::fma(x, y, a0);
+                }
+                ++k;
+            }
+            f[i] = k >= 2 ? m::add(a0, a1) : a0;
         }
-        int off = g.k_nnz;
-        for (int e = 0; e < g.g_nnz; ++e) {
-            const int* ix = gi + 3 * e;
-            f[ix[0]] = m::fma(m::mul(val(off + e), xs[ix[1]]), xp[ix[2]], f[ix[0]]);
-        }
-        off += g.g_nnz;
-        for (int e = 0; e < g.l_nnz; ++e) {
-            const int* ix = li + 4 * e;
-            const R t = m::mul(m::mul(val(off + e), xs[ix[1]]), xp[ix[2]]);
-            f[ix[0]] = m::fma(t, xp[ix[3]], f[ix[0]]);
-        }
-        off += g.l_nnz;
-        for (int e = 0; e < g.p_nnz; ++e) {
-            const int* ix = pi + 5 * e;
-            const R t = m::mul(m::mul(m::mul(val(off + e), xs[ix[1]]), xp[ix[2]]), xp[ix[3]]);
-            f[ix[0]] = m::fma(t, xp[ix[4]], f[ix[0]]);
-        }
-        off += g.p_nnz;
-        if (FORCE)
-            for (int e = 0; e < g.f_nnz; ++e) f[fi[e]] = m::fma(val(off + e), u, f[fi[e]]);
     }
 
     // out = J(y)^T w ; pb += (df/dp)^T w  (forward systems: xs == xp == y).
@@ -275,6 +298,126 @@ __device__ __forceinline__ void fwd_run(const Sys& sys, const FwdArgs<R>& a, int
         int slot = 0;
 #pragma unroll
         for (int i = 0; i < n; ++i)
+            if (i < 64 && ((max_mask >> i) & 1ull)) { a.out_max[slot * B + b] = Mx[i]; ++slot; }
+    }
+    if (HSQ) a.out_sq[b] = sq;
+}
+
+// Flat read of the excitation table, 0 past its end.
+template <typename R>
+__device__ __forceinline__ R sample_at(const Forcing<R>& f, long long idx) {
+    return idx < f.total ? f.x[idx] : R(0);
+}
+
+// Forward integration walking the excitation one sample interval at a time
+// (pattern-specialised kernels).  WP::W is the interpolation window (0 =
+// sample and hold) and WP::wn(i) / WP::wc(i) its next / current-sample
+// weights, compile-time constants, so the W/2 steps of an interval need no
+// index arithmetic; the three samples of the sliding window live in
+// registers and the next one is loaded an interval ahead.  Every forcing
+// value equals force_at's (same operations on the same operands); steps
+// before the first and after the last whole interval use force_at.
+template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, class WP, class Sys, class V>
+__device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, int b,
+                                           unsigned long long max_mask, unsigned long long sq_mask,
+                                           V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx) {
+    typedef M<R> m;
+    constexpr int W = WP::W;
+    constexpr unsigned SPI = W == 0 ? 1u : (unsigned)(W / 2);
+    const long long B = a.B;
+    const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+    const unsigned len = a.frc.len;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        Q[i] = a.state[i * B + b];
+        if (KAHAN) Cm[i] = R(0);
+        if (HMAX) Mx[i] = R(0);
+    }
+    R sq = R(0), sqc = R(0);
+    auto post = [&](unsigned step) {
+        if (HTRAJ && step % (unsigned)a.traj_every == 0u) {
+            const long long slot = (long long)(step / (unsigned)a.traj_every) -
+                                   (long long)(a.step0 / (unsigned)a.traj_every) -
+                                   ((a.step0 % (unsigned)a.traj_every) ? 1 : 0);
+            if (slot >= 0 && slot < a.traj_slots) {
+#pragma unroll
+                for (int i = 0; i < N; ++i) a.traj[(slot * N + i) * B + b] = Q[i];
+            }
+        }
+        if (HMAX && (long long)step >= (long long)a.max_start) {
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+                if (i < 64 && ((max_mask >> i) & 1ull)) Mx[i] = m::max(Mx[i], m::abs(Q[i]));
+        }
+        if (HSQ && (long long)step >= (long long)a.sq_start) {
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+                if (i < 64 && ((sq_mask >> i) & 1ull)) {
+                    const R q = Q[i];
+                    if (KAHAN) {
+                        const R y = m::sub(m::mul(q, q), sqc);
+                        const R t = m::add(sq, y);
+                        sqc = m::sub(m::sub(t, sq), y);
+                        sq = t;
+                    } else {
+                        sq = m::fma(q, q, sq);
+                    }
+                }
+        }
+    };
+    unsigned s = a.step0;
+    const unsigned end = a.step0 + (unsigned)a.nsteps;
+    while (s < end && (s % SPI) != 0u) {
+        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, force_at(a.frc, ebase, s, 0u, 0u),
+                              force_at(a.frc, ebase, s, 0u, 1u), force_at(a.frc, ebase, s, 1u, 0u), a.h, a.h2,
+                              a.h6);
+        post(s);
+        ++s;
+    }
+    if (end - s >= SPI) {
+        unsigned j = s / SPI;
+        R x0 = sample_at(a.frc, ebase + j), x1 = sample_at(a.frc, ebase + j + 1), x2 = sample_at(a.frc, ebase + j + 2);
+        for (; end - s >= SPI; s += SPI, ++j) {
+            const R nxt = sample_at(a.frc, ebase + j + 3);
+            const bool g0 = j > 0u && j < len;
+            const bool g1 = j + 1u > 0u && j + 1u < len;
+            R uc;
+            if (W == 0) uc = g0 ? x0 : R(0);
+            else uc = g0 ? m::fma(WP::wc(0), x0, m::mul(WP::wn(0), x1)) : R(0);
+#pragma unroll
+            for (int r = 0; r < (int)SPI; ++r) {
+                const R ua = uc;
+                R ub, un;
+                if (W == 0) {
+                    ub = ua;
+                    un = g1 ? x1 : R(0);
+                } else {
+                    ub = g0 ? m::fma(WP::wc(2 * r + 1), x0, m::mul(WP::wn(2 * r + 1), x1)) : R(0);
+                    if (2 * r + 2 < W) un = g0 ? m::fma(WP::wc(2 * r + 2), x0, m::mul(WP::wn(2 * r + 2), x1)) : R(0);
+                    else un = g1 ? m::fma(WP::wc(0), x1, m::mul(WP::wn(0), x2)) : R(0);
+                }
+                rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6);
+                post(s + (unsigned)r);
+                uc = un;
+            }
+            x0 = x1;
+            x1 = x2;
+            x2 = nxt;
+        }
+    }
+    while (s < end) {
+        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, force_at(a.frc, ebase, s, 0u, 0u),
+                              force_at(a.frc, ebase, s, 0u, 1u), force_at(a.frc, ebase, s, 1u, 0u), a.h, a.h2,
+                              a.h6);
+        post(s);
+        ++s;
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) a.state[i * B + b] = Q[i];
+    if (HMAX) {
+        int slot = 0;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
             if (i < 64 && ((max_mask >> i) & 1ull)) { a.out_max[slot * B + b] = Mx[i]; ++slot; }
     }
     if (HSQ) a.out_sq[b] = sq;

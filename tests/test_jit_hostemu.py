@@ -1,0 +1,69 @@
+"""CPU check of the code generator: the NVRTC source of the pattern-specialised
+forward kernel is compiled for the host (tests/hostemu/emu_main.cpp replaces
+the CUDA intrinsics by correctly rounded host arithmetic) and must equal the
+oracle bit for bit.  Covers the interval loop (prologue, whole intervals,
+epilogue), the literal folding and the canonical accumulation order without
+a GPU."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from pasif_gb300 import synth
+from pasif_gb300.batch import Plan
+from tests import cases
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "pasif_gb300", "csrc")
+
+
+def run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, h, step0, nsteps, prec):
+    if shutil.which("g++") is None:
+        pytest.skip("no host C++ compiler")
+    src = Plan(pat, prec).jit_report(vals, window=W, im=im).split("// ---- source ----\n", 1)[1]
+    d = str(tmp_path)
+    open(os.path.join(d, "gen.cu"), "w").write(src)
+    exe = os.path.join(d, "emu")
+    r = subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", f"-DGEN_SOURCE=\"gen.cu\"", "-I", CSRC,
+                        "-I", d, os.path.join(HERE, "hostemu", "emu_main.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    dt = np.float64 if prec == "fp64" else np.float32
+    B = vals.shape[0]
+    np.ascontiguousarray(vals.T.astype(dt)).tofile(os.path.join(d, "vals.bin"))
+    np.ascontiguousarray(x0.T.astype(dt)).tofile(os.path.join(d, "x0.bin"))
+    np.asarray(exc, np.int32).tofile(os.path.join(d, "exc.bin"))
+    np.asarray(x, dt).tofile(os.path.join(d, "x.bin"))
+    (np.asarray(im, dt).reshape(-1) if W else np.zeros(0, dt)).tofile(os.path.join(d, "im.bin"))
+    xs = np.asarray(x)
+    r = subprocess.run([exe, d, str(B), str(pat.n), str(pat.P), str(xs.shape[0]), str(xs.shape[1]), str(W),
+                        str(step0), str(nsteps), repr(float(h)), "0"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return np.fromfile(os.path.join(d, "out.bin"), dtype=dt).reshape(pat.n, B).T.astype(np.float64)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
+@pytest.mark.parametrize("seed,W,step0,nsteps", [(0, 8, 3, 61), (1, 0, 0, 40), (2, 4, 1, 30), (3, 2, 0, 25)])
+def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps):
+    rng = np.random.default_rng(500 + seed)
+    pat, v = cases.random_system(rng)
+    B = 40
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    x = cases.signals(rng, 3, 28)   # shorter than the run: exercises the gating
+    exc = rng.integers(0, 3, B)
+    im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
+    got = run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, 0.05, step0, nsteps, prec)
+    ref, _, _ = O.batch_forward(pat, vals, x0, exc, x, 0.05, nsteps, W, im, prec, step0)
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_generated_kernel_config2(tmp_path):
+    w = synth.coupled2(n_sys=64, nsteps=300)
+    got = run_emulated(tmp_path, w.pattern, w.values, w.x0, w.exc_index, w.signals, w.window, w.im, w.h, 0, w.nsteps,
+                       "fp32_kahan")
+    ref, _, _ = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
+                                "fp32_kahan")
+    np.testing.assert_array_equal(got, ref)

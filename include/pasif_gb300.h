@@ -213,6 +213,14 @@ int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys,
                           int window, const double* im,
                           char* log, long long capacity, long long* out_len);
 
+/* Same for the pattern-specialised exact-adjoint kernel (sq_mask: components
+ * of the sum-of-squares loss).  Diagnostic; no reference counterpart. */
+int pasif_plan_jit_report_adjoint(const pasif_plan* p, const double* values, int n_sys,
+                                  unsigned long long sq_mask, char* log, long long capacity,
+                                  long long* out_len);
+/* Kernel used by the last pasif_batch_adjoint (PASIF_KERNEL_*). */
+int pasif_batch_adjoint_kernel(pasif_batch* b, int* kind);
+
 /* Measured FMA-pipe throughput of the current GPU in FLOP/s (FMA = 2 FLOP),
  * FP32 (precision != PASIF_FP64) or FP64: the roofline denominator of the
  * FMA-bound RK4 kernels.  Diagnostic; no reference counterpart. */

@@ -109,6 +109,8 @@ _SIGS = {
     "pasif_batch_kernel_info": (C.c_int, [_vp, _ip, _ip]),
     "pasif_plan_jit_report": (C.c_int, [_vp, _dp, C.c_int, C.c_ulonglong, C.c_ulonglong, C.c_int, _dp,
                                         C.c_char_p, C.c_longlong, _llp]),
+    "pasif_plan_jit_report_adjoint": (C.c_int, [_vp, _dp, C.c_int, C.c_ulonglong, C.c_char_p, C.c_longlong, _llp]),
+    "pasif_batch_adjoint_kernel": (C.c_int, [_vp, _ip]),
     "pasif_fma_peak": (C.c_int, [C.c_int, _dp]),
     "pasif_forward_noalloc": (C.c_int, [C.POINTER(PatternC), C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int,
                                         _vp, C.c_double, C.c_int, C.c_int, _vp, _vp]),

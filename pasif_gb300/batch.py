@@ -52,6 +52,16 @@ class Plan:
         N.check(N.lib.pasif_plan_jit_report(*args, buf, ln.value + 1, C.byref(ln)))
         return buf.value.decode()
 
+    def jit_report_adjoint(self, values=None, sq_mask: int = 0) -> str:
+        """Same as jit_report for the specialised exact-adjoint kernel."""
+        v = N.f64(values) if values is not None else None
+        args = (self.handle, N.dptr(v) if v is not None else None, int(v.shape[0]) if v is not None else 0, sq_mask)
+        ln = C.c_longlong()
+        N.check(N.lib.pasif_plan_jit_report_adjoint(*args, None, 0, C.byref(ln)))
+        buf = C.create_string_buffer(ln.value + 1)
+        N.check(N.lib.pasif_plan_jit_report_adjoint(*args, buf, ln.value + 1, C.byref(ln)))
+        return buf.value.decode()
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h:
@@ -158,9 +168,11 @@ class Batch:
                                           _stream(stream)))
 
     def kernel_info(self):
-        k, r = C.c_int(), C.c_int()
+        k, r, a = C.c_int(), C.c_int(), C.c_int()
         N.check(N.lib.pasif_batch_kernel_info(self.handle, C.byref(k), C.byref(r)))
-        return {"kind": {0: "none", 1: "generic", 2: "specialised"}[k.value], "registers": r.value}
+        N.check(N.lib.pasif_batch_adjoint_kernel(self.handle, C.byref(a)))
+        names = {0: "none", 1: "generic", 2: "specialised"}
+        return {"kind": names[k.value], "registers": r.value, "adjoint": names[a.value]}
 
     def __del__(self):
         h = getattr(self, "handle", None)

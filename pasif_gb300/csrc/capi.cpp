@@ -398,6 +398,51 @@ int pasif_batch_kernel_info(pasif_batch* b, int* kind, int* registers) {
     return PASIF_OK;
 }
 
+static pasif::Literals literals_of(const pasif::Pattern& pat, bool f32, const double* values, int n_sys) {
+    const int P = pat.P();
+    pasif::Literals lit;
+    lit.is_lit.assign(P, 0);
+    lit.value.assign(P, 0.0);
+    if (values && n_sys > 0)
+        for (int q = 0; q < P; ++q) {
+            bool same = true;
+            const double v0 = f32 ? (double)(float)values[q] : values[q];
+            for (int b = 1; b < n_sys && same; ++b) {
+                const double v = f32 ? (double)(float)values[(long long)b * P + q] : values[(long long)b * P + q];
+                same = v == v0 && std::signbit(v) == std::signbit(v0);
+            }
+            lit.is_lit[q] = same && std::isfinite(v0);
+            lit.value[q] = v0;
+        }
+    return lit;
+}
+
+int pasif_plan_jit_report_adjoint(const pasif_plan* p, const double* values, int n_sys, unsigned long long sq_mask,
+                                  char* log, long long capacity, long long* out_len) {
+    if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null plan");
+    return guard([&] {
+        const bool f32 = p->p->precision != pasif::kFP64;
+        const std::string src =
+            pasif::adj_source(p->p->pat, literals_of(p->p->pat, f32, values, n_sys), f32, sq_mask);
+        std::string report, err;
+        if (!pasif::compile_report(src, &report, &err)) return fail(PASIF_ERR_NVRTC, err);
+        report += "\n// ---- source ----\n" + src;
+        if (out_len) *out_len = (long long)report.size();
+        if (log && capacity > 0) {
+            const size_t n = std::min<size_t>(report.size(), (size_t)capacity - 1);
+            std::memcpy(log, report.data(), n);
+            log[n] = '\0';
+        }
+        return PASIF_OK;
+    });
+}
+
+int pasif_batch_adjoint_kernel(pasif_batch* b, int* kind) {
+    if (!b || !b->b || !kind) return fail(PASIF_ERR_INVALID, "null handle");
+    *kind = b->b->last_adj_kind;
+    return PASIF_OK;
+}
+
 int pasif_fma_peak(int precision, double* flops_per_second) {
     if (!flops_per_second) return fail(PASIF_ERR_INVALID, "null output");
     cudaError_t e = pk::measure_fma_peak(precision != PASIF_FP64, flops_per_second);

@@ -437,14 +437,30 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     a.kahan = plan->precision == kFP32Kahan ? 1 : 0;                  \
     a.sq_start = red.sq_start;                                        \
     a.sq_mask = g_sq ? sm : 0ull;
+    JitKernel jk;
+    std::string jerr;
+    const bool jit = !plan->generic_only && get_adj_kernel(pat, lit, f, g_sq ? sm : 0ull, &jk, &jerr);
+    if (!jit && !plan->generic_only) last_jit_error = jerr;
+    const dim3 grid((unsigned)((B + 127) / 128));
     if (f) {
         PK_FILL_ADJ(float)
-        e = pk::launch_gen_adj(a, st);
+        if (jit) {
+            void* args[] = {&a};
+            e = cudaLaunchKernel((const void*)jk.fn, grid, dim3(128), args, 0, st);
+        } else {
+            e = pk::launch_gen_adj(a, st);
+        }
     } else {
         PK_FILL_ADJ(double)
-        e = pk::launch_gen_adj(a, st);
+        if (jit) {
+            void* args[] = {&a};
+            e = cudaLaunchKernel((const void*)jk.fn, grid, dim3(128), args, 0, st);
+        } else {
+            e = pk::launch_gen_adj(a, st);
+        }
     }
 #undef PK_FILL_ADJ
+    last_adj_kind = jit ? kSpecialised : kGeneric;
     PK_CUDA(e, "adjoint kernel launch");
     int rc = download_interleaved(pbar.p, B, P, false, 1.0, d_values, memory, adj_stage, st, err);
     if (rc) return rc;

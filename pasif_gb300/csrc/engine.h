@@ -87,6 +87,7 @@ struct Batch {
     int max_exc_ = -1;
     double last_h = 0.0;          // time step of the last forward (scales sum q^2)
     int last_kind = kNone;
+    int last_adj_kind = kNone;
     JitKernel last_jit;
     std::string last_jit_error;
 

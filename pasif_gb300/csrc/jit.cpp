@@ -215,6 +215,147 @@ bool fwd_compile_report(const Pattern& pat, const Literals& lit, const FwdKernel
     return to_cubin(fwd_source(pat, lit, key), &cubin, report, err);
 }
 
+namespace {
+
+// JSys members shared by the forward and adjoint programs: values, load, rhs.
+void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32) {
+    o << "#include \"rk4_core.cuh\"\n";
+    o << "namespace pk {\n";
+    o << "typedef " << (f32 ? "float" : "double") << " R;\n";
+    o << "struct JSys {\n";
+    o << "  R p[" << (em.nload > 0 ? em.nload : 1) << "];\n";
+    o << "  __device__ static constexpr int dim() { return " << pat.n << "; }\n";
+    o << "  __device__ __forceinline__ void load(const R* __restrict__ vals, long long B, int b) {\n";
+    for (int q = 0; q < pat.P(); ++q)
+        if (em.slot[q] >= 0) o << "    p[" << em.slot[q] << "] = vals[" << q << "LL * B + b];\n";
+    o << "  }\n";
+    o << "  template <bool FORCE, class V, class W, class F>\n";
+    o << "  __device__ __forceinline__ void rhs(const V& xs, const W& xp, R u, F& f) const {\n";
+    o << "    typedef M<R> m;\n    R a, c;\n";
+    o << "    if (FORCE) {\n";
+    em.rhs(o, true);
+    o << "    } else {\n";
+    em.rhs(o, false);
+    o << "    }\n";
+    o << "  }\n";
+}
+
+// VJP body in the operation order of GenSys::vjp (rk4_core.cuh).
+void emit_vjp(std::ostringstream& o, const Pattern& pat, const Emitter& em) {
+    const int n = pat.n;
+    const int go = pat.k_nnz(), lo = go + pat.g_nnz(), po = lo + pat.l_nnz(), fo = po + pat.p_nnz();
+    auto s = [](int v) { return std::to_string(v); };
+    o << "  template <class V, class W, class O, class PB>\n";
+    o << "  __device__ __forceinline__ void vjp(const V& y, const W& w, R u, O& out, PB& pb) const {\n";
+    o << "    typedef M<R> m;\n";
+    for (int i = 0; i < n; ++i) o << "    out[" << i << "] = R(0);\n";
+    for (int i = 0; i < n; ++i)
+        for (int q = pat.k_ptr[i]; q < pat.k_ptr[i + 1]; ++q) {
+            const std::string j = s(pat.k_col[q]);
+            o << "    out[" << j << "] = m::fma(" << em.val(q) << ", w[" << i << "], out[" << j << "]);\n";
+            o << "    pacc_add(pb[" << q << "], w[" << i << "], y[" << j << "]);\n";
+        }
+    for (int e = 0; e < pat.g_nnz(); ++e) {
+        const int* ix = &pat.g_idx[3 * e];
+        const std::string i = s(ix[0]), j = s(ix[1]), k = s(ix[2]);
+        o << "    { const R a_ = m::mul(" << em.val(go + e) << ", w[" << i << "]);\n";
+        o << "      out[" << j << "] = m::fma(a_, y[" << k << "], out[" << j << "]);\n";
+        o << "      out[" << k << "] = m::fma(a_, y[" << j << "], out[" << k << "]);\n";
+        o << "      pacc_add(pb[" << go + e << "], m::mul(w[" << i << "], y[" << j << "]), y[" << k << "]); }\n";
+    }
+    for (int e = 0; e < pat.l_nnz(); ++e) {
+        const int* ix = &pat.l_idx[4 * e];
+        const std::string i = s(ix[0]), j = s(ix[1]), k = s(ix[2]), l = s(ix[3]);
+        o << "    { const R a_ = m::mul(" << em.val(lo + e) << ", w[" << i << "]);\n";
+        o << "      out[" << j << "] = m::fma(m::mul(a_, y[" << k << "]), y[" << l << "], out[" << j << "]);\n";
+        o << "      out[" << k << "] = m::fma(m::mul(a_, y[" << j << "]), y[" << l << "], out[" << k << "]);\n";
+        o << "      out[" << l << "] = m::fma(m::mul(a_, y[" << j << "]), y[" << k << "], out[" << l << "]);\n";
+        o << "      pacc_add(pb[" << lo + e << "], m::mul(m::mul(w[" << i << "], y[" << j << "]), y[" << k
+          << "]), y[" << l << "]); }\n";
+    }
+    for (int e = 0; e < pat.p_nnz(); ++e) {
+        const int* ix = &pat.p_idx[5 * e];
+        const std::string i = s(ix[0]), j = s(ix[1]), k = s(ix[2]), l = s(ix[3]), mm = s(ix[4]);
+        o << "    { const R a_ = m::mul(" << em.val(po + e) << ", w[" << i << "]);\n";
+        o << "      out[" << j << "] = m::fma(m::mul(m::mul(a_, y[" << k << "]), y[" << l << "]), y[" << mm << "], out["
+          << j << "]);\n";
+        o << "      out[" << k << "] = m::fma(m::mul(m::mul(a_, y[" << j << "]), y[" << l << "]), y[" << mm << "], out["
+          << k << "]);\n";
+        o << "      out[" << l << "] = m::fma(m::mul(m::mul(a_, y[" << j << "]), y[" << k << "]), y[" << mm << "], out["
+          << l << "]);\n";
+        o << "      out[" << mm << "] = m::fma(m::mul(m::mul(a_, y[" << j << "]), y[" << k << "]), y[" << l << "], out["
+          << mm << "]);\n";
+        o << "      pacc_add(pb[" << po + e << "], m::mul(m::mul(m::mul(w[" << i << "], y[" << j << "]), y[" << k
+          << "]), y[" << l << "]), y[" << mm << "]); }\n";
+    }
+    for (int e = 0; e < pat.f_nnz(); ++e)
+        o << "    pacc_add(pb[" << fo + e << "], w[" << pat.f_idx[e] << "], u);\n";
+    o << "  }\n";
+}
+
+bool get_cached(const std::string& src, const char* name, int block, JitKernel* out, std::string* err) {
+    Cache& c = cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    auto it = c.fwd.find(src);
+    if (it != c.fwd.end()) {
+        *out = it->second;
+        return true;
+    }
+    JitKernel k;
+    k.block = block;
+    if (!compile(src, name, &k.fn, err)) return false;
+    cudaFuncAttributes attr;
+    if (cudaFuncGetAttributes(&attr, (const void*)k.fn) == cudaSuccess) {
+        k.regs = attr.numRegs;
+        k.local_bytes = (int)attr.localSizeBytes;
+    }
+    c.fwd[src] = k;
+    *out = k;
+    return true;
+}
+
+}  // namespace
+
+bool compile_report(const std::string& src, std::string* report, std::string* err) {
+    std::vector<char> cubin;
+    return to_cubin(src, &cubin, report, err);
+}
+
+std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask) {
+    Emitter em(pat, lit);
+    std::ostringstream o;
+    o << "// generated by pasif_gb300 jit.cpp: exact adjoint, n=" << pat.n << " P=" << pat.P() << "\n";
+    emit_sys_head(o, pat, em, f32);
+    emit_vjp(o, pat, em);
+    o << "};\n}  // namespace pk\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(128) pk_adj(pk::AdjArgs<pk::R> a) {\n";
+    o << "  using namespace pk;\n";
+    o << "  const int b = blockIdx.x * blockDim.x + threadIdx.x;\n";
+    o << "  if (b >= a.B) return;\n";
+    o << "  JSys sys;\n  sys.load(a.vals, (long long)a.B, b);\n";
+    const int P = pat.P() > 0 ? pat.P() : 1;
+    if (f32) {
+        o << "  RegVec<R, " << P << "> pacc;\n";
+        o << "  adj_run_jit<R, " << pat.n << ", " << P << ", " << (sq_mask ? "true" : "false") << ", true>(sys, a, b, "
+          << sq_mask << "ull, pacc);\n";
+    } else {
+        o << "  GVec<double> pacc{a.pbar + b, (long long)a.B};\n";
+        o << "  adj_run_jit<R, " << pat.n << ", " << P << ", " << (sq_mask ? "true" : "false")
+          << ", false>(sys, a, b, " << sq_mask << "ull, pacc);\n";
+    }
+    o << "}\n";
+    return o.str();
+}
+
+bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, JitKernel* out,
+                    std::string* err) {
+    if (pat.n <= 0 || pat.n > kJitMaxN || pat.P() > 1024) {
+        *err = "pattern outside the specialised range";
+        return false;
+    }
+    return get_cached(adj_source(pat, lit, f32, sq_mask), "pk_adj", 128, out, err);
+}
+
 bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, JitKernel* out,
                     std::string* err) {
     if (pat.n <= 0 || pat.n > kJitMaxN) {

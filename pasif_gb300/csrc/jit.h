@@ -43,6 +43,13 @@ std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelK
 bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey& key,
                     JitKernel* out, std::string* err);
 
+// Source and cached kernel of the exact adjoint (AdjArgs) for a pattern.
+std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask);
+bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, JitKernel* out,
+                    std::string* err);
+// Compile a source without loading it (no GPU needed); report = compiler log.
+bool compile_report(const std::string& src, std::string* report, std::string* err);
+
 // Compile the forward kernel without loading it (no GPU needed) and return
 // the compiler's resource report (registers, spills).
 bool fwd_compile_report(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, std::string* report,

@@ -80,6 +80,13 @@ __device__ __forceinline__ R force_at(const Forcing<R>& f, long long ebase, unsi
     return R(0);
 }
 
+// Parameter-gradient accumulation: into FP64 (fma of the FP32 or FP64
+// factors promoted to double) or, for per-step partial sums, in the compute
+// precision.
+__device__ __forceinline__ void pacc_add(double& p, double x, double y) { p = __fma_rn(x, y, p); }
+__device__ __forceinline__ void pacc_add(double& p, float x, float y) { p = __fma_rn((double)x, (double)y, p); }
+__device__ __forceinline__ void pacc_add(float& p, float x, float y) { p = __fmaf_rn(x, y, p); }
+
 // Pattern interpreted from GenPattern, values read from vals[p][B].
 template <typename R>
 struct GenSys {
@@ -167,7 +174,7 @@ struct GenSys {
             for (int p = kp[i]; p < kp[i + 1]; ++p) {
                 const int j = kc[p];
                 out[j] = m::fma(val(p), wi, out[j]);
-                pb[p] = __fma_rn((double)wi, (double)y[j], pb[p]);
+                pacc_add(pb[p], wi, y[j]);
             }
         }
         int off = g.k_nnz;
@@ -177,7 +184,7 @@ struct GenSys {
             const R a = m::mul(val(off + e), wi);
             out[ix[1]] = m::fma(a, yk, out[ix[1]]);
             out[ix[2]] = m::fma(a, yj, out[ix[2]]);
-            pb[off + e] = __fma_rn((double)m::mul(wi, yj), (double)yk, pb[off + e]);
+            pacc_add(pb[off + e], m::mul(wi, yj), yk);
         }
         off += g.g_nnz;
         for (int e = 0; e < g.l_nnz; ++e) {
@@ -187,7 +194,7 @@ struct GenSys {
             out[ix[1]] = m::fma(m::mul(a, yk), yl, out[ix[1]]);
             out[ix[2]] = m::fma(m::mul(a, yj), yl, out[ix[2]]);
             out[ix[3]] = m::fma(m::mul(a, yj), yk, out[ix[3]]);
-            pb[off + e] = __fma_rn((double)m::mul(m::mul(wi, yj), yk), (double)yl, pb[off + e]);
+            pacc_add(pb[off + e], m::mul(m::mul(wi, yj), yk), yl);
         }
         off += g.l_nnz;
         for (int e = 0; e < g.p_nnz; ++e) {
@@ -198,11 +205,11 @@ struct GenSys {
             out[ix[2]] = m::fma(m::mul(m::mul(a, yj), yl), ym, out[ix[2]]);
             out[ix[3]] = m::fma(m::mul(m::mul(a, yj), yk), ym, out[ix[3]]);
             out[ix[4]] = m::fma(m::mul(m::mul(a, yj), yk), yl, out[ix[4]]);
-            pb[off + e] = __fma_rn((double)m::mul(m::mul(m::mul(wi, yj), yk), yl), (double)ym, pb[off + e]);
+            pacc_add(pb[off + e], m::mul(m::mul(m::mul(wi, yj), yk), yl), ym);
         }
         off += g.p_nnz;
         for (int e = 0; e < g.f_nnz; ++e)
-            pb[off + e] = __fma_rn((double)w[fi[e]], (double)u, pb[off + e]);
+            pacc_add(pb[off + e], w[fi[e]], u);
     }
 };
 
@@ -421,6 +428,120 @@ __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, 
             if (i < 64 && ((max_mask >> i) & 1ull)) { a.out_max[slot * B + b] = Mx[i]; ++slot; }
     }
     if (HSQ) a.out_sq[b] = sq;
+}
+
+// Exact discrete adjoint for pattern-specialised kernels: the same algorithm
+// and operation order as adj_run_generic below, with every state-sized vector
+// in registers (N compile-time) and the chunk states in the global buffer.
+// PACC = RegVec<float, P> (FP32: parameter gradients summed per step in FP32,
+// then added to the FP64 totals) or GVec<double> (FP64: straight into the
+// FP64 totals, bit-identical to the generic kernel and the oracle).
+template <typename R, int N, int P, bool HSQ, bool STEP_ACC, class Sys, class PACC>
+__device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a, int b, unsigned long long sq_mask,
+                                            PACC& pacc) {
+    typedef M<R> m;
+    const long long B = a.B;
+    GVec<double> PB{a.pbar + b, B};
+    const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+    RegVec<R, N> Q, Cm, S, K, Mi;
+    for (int p = 0; p < P; ++p) PB[p] = 0.0;
+    if (STEP_ACC) {
+#pragma unroll
+        for (int p = 0; p < P; ++p) pacc[p] = R(0);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) { Q[i] = a.x0[i * B + b]; Cm[i] = R(0); }
+    for (int t = 0; t < a.nsteps; ++t) {
+        if (t % a.C == 0) {
+            R* ck = a.ckpt + (long long)(t / a.C) * 2 * N * B + b;
+#pragma unroll
+            for (int i = 0; i < N; ++i) { ck[i * B] = Q[i]; ck[(N + i) * B] = Cm[i]; }
+        }
+        const unsigned st = (unsigned)t;
+        const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+        const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+        const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+        if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+        else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+    }
+    RegVec<R, N> LAM, QN;
+#pragma unroll
+    for (int i = 0; i < N; ++i) LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0);
+    const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
+    for (int k = a.nck - 1; k >= 0; --k) {
+        const int start = k * a.C;
+        const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
+        const R* ck = a.ckpt + (long long)k * 2 * N * B + b;
+#pragma unroll
+        for (int i = 0; i < N; ++i) { Q[i] = ck[i * B]; Cm[i] = ck[(N + i) * B]; }
+        for (int t = start; t < end; ++t) {
+            R* bt = a.buf + (long long)(t - start) * N * B + b;
+#pragma unroll
+            for (int i = 0; i < N; ++i) bt[i * B] = Q[i];
+            const unsigned st = (unsigned)t;
+            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+            else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+        }
+#pragma unroll
+        for (int i = 0; i < N; ++i) QN[i] = Q[i];
+        for (int t = end - 1; t >= start; --t) {
+            RegVec<R, N> QC, Y2, Y3, Y4, QB, KB, YB;
+            const R* bt = a.buf + (long long)(t - start) * N * B + b;
+#pragma unroll
+            for (int i = 0; i < N; ++i) QC[i] = bt[i * B];
+            if (HSQ && a.g_sq && t >= a.sq_start) {
+#pragma unroll
+                for (int i = 0; i < N; ++i)
+                    if (i < 64 && ((sq_mask >> i) & 1ull)) LAM[i] = m::fma(gsq2h, QN[i], LAM[i]);
+            }
+            const unsigned st = (unsigned)t;
+            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            sys.template rhs<true>(QC, QC, ua, K);
+#pragma unroll
+            for (int i = 0; i < N; ++i) Y2[i] = m::fma(a.h2, K[i], QC[i]);
+            sys.template rhs<true>(Y2, Y2, ub, K);
+#pragma unroll
+            for (int i = 0; i < N; ++i) Y3[i] = m::fma(a.h2, K[i], QC[i]);
+            sys.template rhs<true>(Y3, Y3, ub, K);
+#pragma unroll
+            for (int i = 0; i < N; ++i) { Y4[i] = m::fma(a.h, K[i], QC[i]); KB[i] = m::mul(a.h6, LAM[i]); QB[i] = LAM[i]; }
+            sys.vjp(Y4, KB, uc, YB, pacc);
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h, YB[i], m::mul(R(2), sb));
+            }
+            sys.vjp(Y3, KB, ub, YB, pacc);
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h2, YB[i], m::mul(R(2), sb));
+            }
+            sys.vjp(Y2, KB, ub, YB, pacc);
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h2, YB[i], sb);
+            }
+            sys.vjp(QC, KB, ua, YB, pacc);
+#pragma unroll
+            for (int i = 0; i < N; ++i) { LAM[i] = m::add(QB[i], YB[i]); QN[i] = QC[i]; }
+            if (STEP_ACC) {
+#pragma unroll
+                for (int p = 0; p < P; ++p) { PB[p] = PB[p] + (double)pacc[p]; pacc[p] = R(0); }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) a.dx0[i * B + b] = LAM[i];
 }
 
 // Exact discrete adjoint of the RK4 map for one instance (generic storage):

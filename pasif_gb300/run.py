@@ -28,6 +28,7 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp32_kahan", choices=["fp64", "fp32", "fp32_kahan"])
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--generic", action="store_true", help="use the pattern-interpreting kernel")
+    ap.add_argument("--adjoint", action="store_true", help="run the exact adjoint (gradients) instead")
     a = ap.parse_args(argv)
     kw = {}
     if a.systems:
@@ -39,6 +40,17 @@ def main(argv=None):
     sig = Signals(w.signals, w.window, w.im, a.precision)
     b = Batch(plan, w.values, w.x0, w.exc_index)
     dt = 0.0
+    if a.adjoint:
+        g_sq = np.ones(w.n_sys)
+        for _ in range(max(1, a.repeat)):
+            t0 = time.perf_counter()
+            dv, dx = b.adjoint(sig, w.h, w.nsteps, g_sq=g_sq, sq_comp=w.sq_comp or (0,), sq_start=w.sq_start)
+            dt = time.perf_counter() - t0
+        print(json.dumps({"config": a.config, "systems": w.n_sys, "nsteps": w.nsteps, "precision": a.precision,
+                          "adjoint_seconds_last": dt, "gradients_per_s": w.n_sys / dt,
+                          "adjoint_system_steps_per_s": w.n_sys * w.nsteps / dt,
+                          "checksum": float(np.sum(np.abs(dv)))}))
+        return
     for _ in range(max(1, a.repeat)):
         t0 = time.perf_counter()
         b.forward(sig, w.h, w.nsteps, **w.forward_kwargs())

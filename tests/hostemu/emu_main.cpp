@@ -59,34 +59,83 @@ int main(int argc, char** argv) {
     auto exc = readf<int>(dir, "exc.bin", (size_t)B);
     auto x = readf<R>(dir, "x.bin", (size_t)n_exc * len);
     auto im = readf<R>(dir, "im.bin", (size_t)2 * W);
+    pk::Forcing<R> frc;
+    std::memset(&frc, 0, sizeof frc);
+    frc.x = x.data();
+    frc.im = W ? im.data() : nullptr;
+    frc.total = (long long)n_exc * len;
+    frc.len = (unsigned)len;
+    frc.w = (unsigned)W;
+    while (W && (1u << frc.lw) < (unsigned)W) frc.lw++;
+    blockDim.x = 128;
+    char path[1024];
+#ifndef EMU_ADJ
     pk::FwdArgs<R> a;
     std::memset(&a, 0, sizeof a);
     a.vals = vals.data();
     a.state = state.data();
     a.exc_index = exc.data();
     a.traj_every = 1;
-    a.frc.x = x.data();
-    a.frc.im = W ? im.data() : nullptr;
-    a.frc.total = (long long)n_exc * len;
-    a.frc.len = (unsigned)len;
-    a.frc.w = (unsigned)W;
-    while (W && (1u << a.frc.lw) < (unsigned)W) a.frc.lw++;
+    a.frc = frc;
     a.h = (R)h;
     a.h2 = (R)(h / 2.0);
     a.h6 = (R)(h / 6.0);
     a.B = B;
     a.step0 = step0;
     a.nsteps = nsteps;
-    blockDim.x = 128;
     for (int b = 0; b < B; ++b) {
         blockIdx.x = (unsigned)(b / 128);
         threadIdx.x = (unsigned)(b % 128);
         pk_fwd(a);
     }
-    char path[1024];
     std::snprintf(path, sizeof path, "%s/out.bin", dir);
     FILE* f = std::fopen(path, "wb");
     std::fwrite(state.data(), sizeof(R), state.size(), f);
     std::fclose(f);
+#else
+    // exact adjoint: argv[11] = kahan, argv[12] = sq_start; g_sq.bin, g_final.bin inputs
+    const int kahan = std::atoi(argv[11]);
+    const int sq_start = argc > 12 ? std::atoi(argv[12]) : 0;
+    auto gsq = readf<R>(dir, "gsq.bin", (size_t)B);
+    auto gfin = readf<R>(dir, "gfin.bin", (size_t)n * B);
+    const int C = nsteps > 0 ? (int)std::ceil(std::sqrt((double)nsteps)) : 1;
+    const int nck = nsteps > 0 ? (nsteps + C - 1) / C : 0;
+    std::vector<R> ckpt((size_t)B * 2 * n * (nck > 0 ? nck : 1)), buf((size_t)B * n * C), dx0((size_t)B * n);
+    std::vector<double> pbar((size_t)B * (P > 0 ? P : 1));
+    pk::AdjArgs<R> a;
+    std::memset(&a, 0, sizeof a);
+    a.vals = vals.data();
+    a.x0 = state.data();
+    a.exc_index = exc.data();
+    a.ckpt = ckpt.data();
+    a.buf = buf.data();
+    a.pbar = pbar.data();
+    a.dx0 = dx0.data();
+    a.g_final = gfin.data();
+    a.g_sq = gsq.data();
+    a.frc = frc;
+    a.h = (R)h;
+    a.h2 = (R)(h / 2.0);
+    a.h6 = (R)(h / 6.0);
+    a.B = B;
+    a.nsteps = nsteps;
+    a.C = C;
+    a.nck = nck;
+    a.kahan = kahan;
+    a.sq_start = sq_start;
+    for (int b = 0; b < B; ++b) {
+        blockIdx.x = (unsigned)(b / 128);
+        threadIdx.x = (unsigned)(b % 128);
+        pk_adj(a);
+    }
+    std::snprintf(path, sizeof path, "%s/pbar.bin", dir);
+    FILE* f = std::fopen(path, "wb");
+    std::fwrite(pbar.data(), sizeof(double), pbar.size(), f);
+    std::fclose(f);
+    std::snprintf(path, sizeof path, "%s/dx0.bin", dir);
+    f = std::fopen(path, "wb");
+    std::fwrite(dx0.data(), sizeof(R), dx0.size(), f);
+    std::fclose(f);
+#endif
     return 0;
 }

@@ -11,14 +11,17 @@ from tests import cases
 pytestmark = pytest.mark.gpu
 
 
-def gpu_adjoint(pat, vals, x0, exc, x, h, N, W, im, prec, gf, gs, sq_comp, sq_start):
-    plan = Plan(pat, prec)
+def gpu_adjoint(pat, vals, x0, exc, x, h, N, W, im, prec, gf, gs, sq_comp, sq_start, generic=False):
+    plan = Plan(pat, prec, generic_only=generic)
     b = Batch(plan, vals, x0, exc)
-    return b.adjoint(Signals(x, W, im, prec), h, N, g_final=gf, g_sq=gs, sq_comp=sq_comp, sq_start=sq_start)
+    out = b.adjoint(Signals(x, W, im, prec), h, N, g_final=gf, g_sq=gs, sq_comp=sq_comp, sq_start=sq_start)
+    assert b.kernel_info()["adjoint"] == ("generic" if generic else "specialised")
+    return out
 
 
+@pytest.mark.parametrize("generic", [False, True])
 @pytest.mark.parametrize("seed", range(3))
-def test_adjoint_bit_exact_fp64(gpu, seed):
+def test_adjoint_bit_exact_fp64(gpu, seed, generic):
     rng = np.random.default_rng(300 + seed)
     pat, v = cases.random_system(rng)
     B = 40
@@ -29,7 +32,7 @@ def test_adjoint_bit_exact_fp64(gpu, seed):
     gf = rng.normal(size=(B, pat.n))
     gs = rng.normal(size=B)
     sq = (0,)
-    dv, dx = gpu_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, [[0, .5], [1, .5]], "fp64", gf, gs, sq, N // 3)
+    dv, dx = gpu_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, [[0, .5], [1, .5]], "fp64", gf, gs, sq, N // 3, generic)
     odv, odx = O.batch_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, [[0, .5], [1, .5]], gf, gs, sq, N // 3)
     np.testing.assert_array_equal(dv, odv)
     np.testing.assert_array_equal(dx, odx)

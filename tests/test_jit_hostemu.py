@@ -60,6 +60,50 @@ def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps)
     np.testing.assert_array_equal(got, ref)
 
 
+@pytest.mark.parametrize("seed", range(3))
+def test_generated_adjoint_matches_oracle(tmp_path, seed):
+    """FP64 specialised adjoint (registers + FP64 gradient totals) equals the
+    oracle's exact discrete adjoint bit for bit."""
+    if shutil.which("g++") is None:
+        pytest.skip("no host C++ compiler")
+    rng = np.random.default_rng(700 + seed)
+    pat, v = cases.random_system(rng)
+    B = 24
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    x = cases.signals(rng, 2, 90)
+    exc = rng.integers(0, 2, B)
+    N = [37, 64, 101][seed]
+    sq = (0,) if pat.n == 1 else (0, pat.n - 1)
+    mask = sum(1 << c for c in sq)
+    gf = rng.normal(size=(B, pat.n))
+    gs = rng.normal(size=B)
+    src = Plan(pat, "fp64").jit_report_adjoint(vals, sq_mask=mask).split("// ---- source ----\n", 1)[1]
+    d = str(tmp_path)
+    open(os.path.join(d, "gen.cu"), "w").write(src)
+    exe = os.path.join(d, "emu")
+    r = subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-DEMU_ADJ", f"-DGEN_SOURCE=\"gen.cu\"",
+                        "-I", CSRC, "-I", d, os.path.join(HERE, "hostemu", "emu_main.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    np.ascontiguousarray(vals.T).tofile(os.path.join(d, "vals.bin"))
+    np.ascontiguousarray(x0.T).tofile(os.path.join(d, "x0.bin"))
+    np.asarray(exc, np.int32).tofile(os.path.join(d, "exc.bin"))
+    np.asarray(x, np.float64).tofile(os.path.join(d, "x.bin"))
+    np.zeros(2 * 2).tofile(os.path.join(d, "im.bin"))
+    np.ascontiguousarray(gs).tofile(os.path.join(d, "gsq.bin"))
+    np.ascontiguousarray(gf.T).tofile(os.path.join(d, "gfin.bin"))
+    im = np.array([[0, .5], [1, .5]])
+    im.tofile(os.path.join(d, "im.bin"))
+    r = subprocess.run([exe, d, str(B), str(pat.n), str(pat.P), "2", "90", "2", "0", str(N), repr(0.03), "0",
+                        str(N // 3)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    pbar = np.fromfile(os.path.join(d, "pbar.bin")).reshape(pat.P, B).T
+    dx0 = np.fromfile(os.path.join(d, "dx0.bin")).reshape(pat.n, B).T
+    odv, odx = O.batch_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, im, gf, gs, sq, N // 3)
+    np.testing.assert_array_equal(pbar, odv)
+    np.testing.assert_array_equal(dx0, odx)
+
+
 def test_generated_kernel_config2(tmp_path):
     w = synth.coupled2(n_sys=64, nsteps=300)
     got = run_emulated(tmp_path, w.pattern, w.values, w.x0, w.exc_index, w.signals, w.window, w.im, w.h, 0, w.nsteps,

@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--systems", type=int, default=16384)
     ap.add_argument("--nsteps", type=int, default=200_000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--serve", type=float, default=1.5, help="seconds of served-stream arrivals (0: skip)")
     return ap.parse_args()
 
 
@@ -267,6 +268,35 @@ def main():
     rms32, rms64 = np.sqrt(st32[:, 4] / T), np.sqrt(st64[:, 4] / T)
     rel = np.abs(rms32 - rms64) / np.abs(rms64)
 
+    # adjoint gradients/s: 8-DOF chain, 4096 systems x 50000 steps, gradients of
+    # the final-half sum of squared positions w.r.t. every value (FP32 + FP64 check)
+    from pasif_gb300 import synth
+    c3 = synth.chain8()
+    adj = {}
+    grads = {}
+    for prec in ("fp32_kahan", "fp64"):
+        pl = Plan(c3.pattern, prec)
+        sg = Signals(c3.signals, c3.window, c3.im, prec, stream=stream)
+        bt = Batch(pl, c3.values, c3.x0, c3.exc_index, stream=stream)
+        gsq = np.ones(c3.n_sys)
+        bt.adjoint(sg, c3.h, 200, g_sq=gsq, sq_comp=c3.sq_comp, sq_start=100, stream=stream)   # warm (NVRTC)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dv, _ = bt.adjoint(sg, c3.h, c3.nsteps, g_sq=gsq, sq_comp=c3.sq_comp, sq_start=c3.sq_start, stream=stream)
+        dt = time.perf_counter() - t0
+        grads[prec] = dv
+        adj[prec] = {"gradients_per_s": c3.n_sys / dt, "adjoint_system_steps_per_s": c3.n_sys * c3.nsteps / dt,
+                     "seconds": dt, "kernel": bt.kernel_info()["adjoint"]}
+    g32, g64 = grads["fp32_kahan"], grads["fp64"]
+    grel = np.abs(g32 - g64) / (np.abs(g64) + 1e-6 * np.abs(g64).max())
+
+    # served mixed stream: Poisson 200 req/s, 70/30 forward/adjoint, 1-4096
+    # systems of DOF 1..64, 1e4-2e5 steps (continuous batching, p50/p99)
+    served = None
+    if args.serve > 0 and rank == 0:
+        from pasif_gb300 import serve
+        served = serve.run(rate=200.0, duration=args.serve, seed=5)
+
     # roofline: algorithmic FLOPs per launch / launch time vs the measured FMA peak
     flops_ss = w.pattern.flops_per_step()
     achieved = flops_ss * sys_steps / (kernel_s / args.steps)
@@ -293,6 +323,12 @@ def main():
                 "fp64_path": {"value": fp64_value, "unit": UNIT, "speedup_fp32_kahan": value / world / fp64_value},
                 "accuracy": {"max_rel_err_rms_fp32_kahan_vs_fp64": float(rel.max()),
                              "median_rel_err": float(np.median(rel)), "bound": 1e-5},
+                "adjoint": {"workload": "chain_8dof: 4096 systems x 50000 steps, exact discrete adjoint, "
+                                        "gradients w.r.t. all 43 values per system (wall time of the C-ABI call)",
+                            "fp32_kahan": adj["fp32_kahan"], "fp64": adj["fp64"],
+                            "max_rel_err_grad_fp32_kahan_vs_fp64": float(grel.max()),
+                            "median_rel_err_grad": float(np.median(grel))},
+                "serving": served,
                 "wall_s_timed_region": t_wall}
         if world == 1:
             rate, n_s, dt = cpu_sample_rate(w, args.cpu_seconds, host_threads())

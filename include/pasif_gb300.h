@@ -46,6 +46,9 @@ extern "C" {
 #define PASIF_KERNEL_SPECIALISED 2  /* NVRTC kernel specialised to pattern  */
 
 #define PASIF_PLAN_GENERIC_ONLY 1   /* plan flag: never specialise          */
+#define PASIF_PLAN_NO_LITERALS 2    /* plan flag: specialise to the pattern
+                                       only, load every value (one compiled
+                                       kernel serves all batches of a plan) */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* pasif_last_error(void);
@@ -171,7 +174,8 @@ typedef struct pasif_signals pasif_signals;
 typedef struct pasif_batch pasif_batch;
 
 /* Plan = pattern + precision (the pattern-specialised kernels are compiled
- * lazily, per batch, by the first solve).  flags: PASIF_PLAN_GENERIC_ONLY. */
+ * lazily, per batch, by the first solve).  flags: PASIF_PLAN_GENERIC_ONLY,
+ * PASIF_PLAN_NO_LITERALS. */
 int pasif_plan_create(pasif_plan** out, const pasif_pattern* pattern, int precision, int flags);
 int pasif_plan_destroy(pasif_plan* p);
 
@@ -212,6 +216,41 @@ int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys,
                           unsigned long long max_mask, unsigned long long sq_mask,
                           int window, const double* im,
                           char* log, long long capacity, long long* out_len);
+
+/* ======================================================================
+ * Serving pools: continuous batching of forward requests (no reference
+ * counterpart; the reference solves one configured system set per call).
+ * A pool holds `capacity` slots of one pattern class (pattern, precision,
+ * forcing window/weights, time step h, reducer components) and a signal
+ * arena of `arena_samples` samples.  A request of n_sys systems takes n_sys
+ * free slots; each pasif_pool_launch advances every busy slot by up to
+ * `chunk` steps from its own step index (one CUDA-graph replay), so requests
+ * join and leave between chunks while others run.  Every slot computes what
+ * a one-request batch computes, bit for bit.
+ * ====================================================================== */
+typedef struct pasif_pool pasif_pool;
+int pasif_pool_create(pasif_pool** out, const pasif_pattern* pattern, int precision, int window,
+                      const double* im, double h, const pasif_reducers* red, int capacity,
+                      long long arena_samples, int chunk);
+int pasif_pool_destroy(pasif_pool* p);
+/* Host arrays: values[n_sys][P], x0[n_sys][n], exc_index[n_sys],
+ * signals[n_exc][len]; integrates nsteps from step 0.  PASIF_ERR_STATE when
+ * slots or arena space are short (retry after a harvest). */
+int pasif_pool_admit(pasif_pool* p, int n_sys, const double* values, const double* x0,
+                     const int* exc_index, const double* signals, int n_exc, int len, int nsteps,
+                     int max_start, int sq_start, int* request_id);
+/* One chunk for every busy slot (asynchronous, on the pool's own stream). */
+int pasif_pool_launch(pasif_pool* p);
+/* Waits for the pool's stream; lists requests whose slots have all finished. */
+int pasif_pool_poll(pasif_pool* p, int* finished, int capacity, int* n_finished);
+/* Results of a finished request (state[n_sys][n], max[n_sys][n_max],
+ * sq[n_sys]; any may be NULL); frees its slots and arena space. */
+int pasif_pool_harvest(pasif_pool* p, int request_id, double* state, double* max, double* sq);
+int pasif_pool_info(pasif_pool* p, int* free_slots, long long* free_arena, int* active);
+/* Compile (no GPU needed) the pool chunk kernel a pool of this plan would
+ * use; compiler report then the source after "// ---- source ----". */
+int pasif_plan_jit_report_pool(const pasif_plan* p, int window, const double* im, const pasif_reducers* red,
+                               char* log, long long capacity, long long* out_len);
 
 /* Same for the pattern-specialised exact-adjoint kernel (sq_mask: components
  * of the sum-of-squares loss).  Diagnostic; no reference counterpart. */

@@ -26,6 +26,7 @@ FP64, FP32, FP32_KAHAN = 0, 1, 2
 HOST, DEVICE = 0, 1
 KERNEL_NONE, KERNEL_GENERIC, KERNEL_SPECIALISED = 0, 1, 2
 PLAN_GENERIC_ONLY = 1
+PLAN_NO_LITERALS = 2
 
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32_kahan": FP32_KAHAN}
 
@@ -111,6 +112,17 @@ _SIGS = {
                                         C.c_char_p, C.c_longlong, _llp]),
     "pasif_plan_jit_report_adjoint": (C.c_int, [_vp, _dp, C.c_int, C.c_ulonglong, C.c_char_p, C.c_longlong, _llp]),
     "pasif_batch_adjoint_kernel": (C.c_int, [_vp, _ip]),
+    "pasif_pool_create": (C.c_int, [C.POINTER(_vp), C.POINTER(PatternC), C.c_int, C.c_int, _dp, C.c_double,
+                                    C.POINTER(ReducersC), C.c_int, C.c_longlong, C.c_int]),
+    "pasif_pool_destroy": (C.c_int, [_vp]),
+    "pasif_pool_admit": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   _ip]),
+    "pasif_pool_launch": (C.c_int, [_vp]),
+    "pasif_pool_poll": (C.c_int, [_vp, _ip, C.c_int, _ip]),
+    "pasif_pool_harvest": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
+    "pasif_pool_info": (C.c_int, [_vp, _ip, _llp, _ip]),
+    "pasif_plan_jit_report_pool": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(ReducersC), C.c_char_p, C.c_longlong,
+                                             _llp]),
     "pasif_fma_peak": (C.c_int, [C.c_int, _dp]),
     "pasif_forward_noalloc": (C.c_int, [C.POINTER(PatternC), C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int,
                                         _vp, C.c_double, C.c_int, C.c_int, _vp, _vp]),

@@ -29,13 +29,15 @@ def _stream(stream) -> C.c_void_p:
 
 
 class Plan:
-    def __init__(self, pattern: Pattern, precision="fp64", generic_only: bool = False):
+    def __init__(self, pattern: Pattern, precision="fp64", generic_only: bool = False, literals: bool = True):
+        """literals=False: the specialised kernels load every value, so one
+        compiled kernel serves every batch of the plan (serving)."""
         self.pattern = pattern
         self.precision = _prec(precision)
         self._c = pattern.to_c()
         h = C.c_void_p()
-        N.check(N.lib.pasif_plan_create(C.byref(h), C.byref(self._c), self.precision,
-                                        N.PLAN_GENERIC_ONLY if generic_only else 0))
+        flags = (N.PLAN_GENERIC_ONLY if generic_only else 0) | (0 if literals else N.PLAN_NO_LITERALS)
+        N.check(N.lib.pasif_plan_create(C.byref(h), C.byref(self._c), self.precision, flags))
         self.handle = h
 
     def jit_report(self, values=None, max_mask: int = 0, sq_mask: int = 0, window: int = 0, im=None) -> str:
@@ -50,6 +52,17 @@ class Plan:
         N.check(N.lib.pasif_plan_jit_report(*args, None, 0, C.byref(ln)))
         buf = C.create_string_buffer(ln.value + 1)
         N.check(N.lib.pasif_plan_jit_report(*args, buf, ln.value + 1, C.byref(ln)))
+        return buf.value.decode()
+
+    def jit_report_pool(self, window: int = 0, im=None, max_comp=(), sq_comp=()) -> str:
+        """Same as jit_report for the serving-pool chunk kernel."""
+        w = N.f64(im).reshape(-1) if im is not None else None
+        red = reducers_c(max_comp, 0, sq_comp, 0)
+        args = (self.handle, int(window), N.dptr(w) if w is not None else None, C.byref(red))
+        ln = C.c_longlong()
+        N.check(N.lib.pasif_plan_jit_report_pool(*args, None, 0, C.byref(ln)))
+        buf = C.create_string_buffer(ln.value + 1)
+        N.check(N.lib.pasif_plan_jit_report_pool(*args, buf, ln.value + 1, C.byref(ln)))
         return buf.value.decode()
 
     def jit_report_adjoint(self, values=None, sq_mask: int = 0) -> str:

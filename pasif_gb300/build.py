@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUD
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["generic_kernels.cu", "noalloc.cu"]
-CPP_SOURCES = ["engine.cpp", "jit.cpp", "driver.cpp", "capi.cpp", "pattern.cpp"]
+CPP_SOURCES = ["engine.cpp", "jit.cpp", "driver.cpp", "capi.cpp", "pattern.cpp", "pool.cpp"]
 EMBEDDED = ["pk_args.h", "rk4_core.cuh"]
 
 

@@ -13,6 +13,7 @@
 
 #include "driver.h"
 #include "generic_kernels.h"
+#include "pool.h"
 #include "engine.h"
 
 struct pasif_driver {
@@ -27,6 +28,9 @@ struct pasif_signals {
 struct pasif_batch {
     std::unique_ptr<pasif::Batch> b;
     int n_max = 0;
+};
+struct pasif_pool {
+    std::unique_ptr<pasif::Pool> p;
 };
 
 namespace {
@@ -304,6 +308,7 @@ int pasif_plan_create(pasif_plan** out, const pasif_pattern* pattern, int precis
         std::unique_ptr<pasif_plan> h(new pasif_plan());
         int rc = pasif::plan_create(pat, precision, (flags & PASIF_PLAN_GENERIC_ONLY) != 0, &h->p, &err);
         if (rc) return fail(rc, err);
+        h->p->no_literals = (flags & PASIF_PLAN_NO_LITERALS) != 0;
         *out = h.release();
         return PASIF_OK;
     });
@@ -396,6 +401,113 @@ int pasif_batch_kernel_info(pasif_batch* b, int* kind, int* registers) {
     if (kind) *kind = b->b->last_kind;
     if (registers) *registers = b->b->last_kind == pasif::kSpecialised ? b->b->last_jit.regs : 0;
     return PASIF_OK;
+}
+
+/* ---------------- serving pools ---------------- */
+
+int pasif_pool_create(pasif_pool** out, const pasif_pattern* pattern, int precision, int window, const double* im,
+                      double h, const pasif_reducers* red, int capacity, long long arena_samples, int chunk) {
+    return guard([&] {
+        if (!out) return fail(PASIF_ERR_INVALID, "null output handle");
+        pasif::Pattern pat;
+        std::string err;
+        if (!to_pattern(pattern, &pat, &err)) return fail(PASIF_ERR_INVALID, err);
+        pasif::Reducers r;
+        if (!to_reducers(red, &r, &err)) return fail(PASIF_ERR_INVALID, err);
+        std::unique_ptr<pasif_pool> h_(new pasif_pool());
+        int rc = pasif::Pool::create(pat, precision, window, im, h, r.max_comp, r.sq_comp, capacity, arena_samples,
+                                     chunk, &h_->p, &err);
+        if (rc) return fail(rc, err);
+        *out = h_.release();
+        return PASIF_OK;
+    });
+}
+
+int pasif_pool_destroy(pasif_pool* p) {
+    delete p;
+    return PASIF_OK;
+}
+
+int pasif_pool_admit(pasif_pool* p, int n_sys, const double* values, const double* x0, const int* exc_index,
+                     const double* signals, int n_exc, int len, int nsteps, int max_start, int sq_start,
+                     int* request_id) {
+    if (!p || !p->p || !request_id) return fail(PASIF_ERR_INVALID, "null handle");
+    return guard([&] {
+        std::string err;
+        return done(p->p->admit(n_sys, values, x0, exc_index, signals, n_exc, len, nsteps, max_start, sq_start,
+                                request_id, &err),
+                    err);
+    });
+}
+
+int pasif_pool_launch(pasif_pool* p) {
+    if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null handle");
+    std::string err;
+    return done(p->p->launch(&err), err);
+}
+
+int pasif_pool_poll(pasif_pool* p, int* finished, int capacity, int* n_finished) {
+    if (!p || !p->p || !n_finished) return fail(PASIF_ERR_INVALID, "null handle");
+    return guard([&] {
+        std::vector<int> f;
+        std::string err;
+        int rc = p->p->poll(&f, &err);
+        if (rc) return fail(rc, err);
+        *n_finished = (int)f.size();
+        if (finished) {
+            if (capacity < (int)f.size()) return fail(PASIF_ERR_INVALID, "finished list capacity too small");
+            std::copy(f.begin(), f.end(), finished);
+        }
+        return PASIF_OK;
+    });
+}
+
+int pasif_pool_harvest(pasif_pool* p, int request_id, double* state, double* max, double* sq) {
+    if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null handle");
+    return guard([&] {
+        std::string err;
+        return done(p->p->harvest(request_id, state, max, sq, &err), err);
+    });
+}
+
+int pasif_pool_info(pasif_pool* p, int* free_slots, long long* free_arena, int* active) {
+    if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null handle");
+    if (free_slots) *free_slots = p->p->free_slots();
+    if (free_arena) *free_arena = p->p->free_arena();
+    if (active) *active = p->p->active();
+    return PASIF_OK;
+}
+
+int pasif_plan_jit_report_pool(const pasif_plan* p, int window, const double* im, const pasif_reducers* red,
+                               char* log, long long capacity, long long* out_len) {
+    if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null plan");
+    return guard([&] {
+        std::string err;
+        pasif::Reducers r;
+        if (!to_reducers(red, &r, &err)) return fail(PASIF_ERR_INVALID, err);
+        if (window < 0 || (window > 0 && (!im || (window & (window - 1)))))
+            return fail(PASIF_ERR_INVALID, "window must be 0 or a power of two with weights");
+        const bool f32 = p->p->precision != pasif::kFP64;
+        pasif::FwdKernelKey key;
+        key.f32 = f32;
+        key.kahan = p->p->precision == pasif::kFP32Kahan;
+        for (int c : r.max_comp) key.max_mask |= 1ull << c;
+        for (int c : r.sq_comp) key.sq_mask |= 1ull << c;
+        key.window = window;
+        for (int i = 0; i < 2 * window; ++i)
+            (i < window ? key.wn : key.wc).push_back(f32 ? (double)(float)im[i] : im[i]);
+        const std::string src = pasif::pool_source(p->p->pat, key);
+        std::string report;
+        if (!pasif::compile_report(src, &report, &err)) return fail(PASIF_ERR_NVRTC, err);
+        report += "\n// ---- source ----\n" + src;
+        if (out_len) *out_len = (long long)report.size();
+        if (log && capacity > 0) {
+            const size_t n = std::min<size_t>(report.size(), (size_t)capacity - 1);
+            std::memcpy(log, report.data(), n);
+            log[n] = '\0';
+        }
+        return PASIF_OK;
+    });
 }
 
 static pasif::Literals literals_of(const pasif::Pattern& pat, bool f32, const double* values, int n_sys) {

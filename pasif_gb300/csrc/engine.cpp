@@ -207,7 +207,7 @@ int Batch::set(const double* values, const double* x0h, const int* exc_index, in
     // values shared by every instance become compile-time constants
     lit.is_lit.assign(P, 0);
     lit.value.assign(P, 0.0);
-    if (memory == kHost && B > 0) {
+    if (memory == kHost && B > 0 && !plan->no_literals) {
         for (int q = 0; q < P; ++q) {
             bool same = true;
             if (f) {

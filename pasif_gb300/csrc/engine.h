@@ -60,7 +60,8 @@ struct Plan {
     Pattern pat;
     int precision = kFP64;
     bool generic_only = false;
-    DevBuf gpat;            // flat pattern for the generic kernels (uploaded on first use)
+    bool no_literals = false;   // every value loaded: one kernel for all batches
+    DevBuf gpat;           // flat pattern for the generic kernels (uploaded on first use)
     pk::GenPattern gen() const;
     int ensure_device(std::string* err);
 };

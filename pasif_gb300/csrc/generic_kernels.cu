@@ -198,3 +198,70 @@ cudaError_t measure_fma_peak(bool f32, double* flops_per_s) {
 }
 
 }  // namespace pk
+
+// ---- serving-pool helpers: scatter new requests into slots, gather results
+
+namespace pk {
+
+template <typename R>
+__global__ void scatter_cols_kernel(const double* __restrict__ src, R* __restrict__ dst, const int* __restrict__ slots,
+                                    int m, int k, long long C) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m * k) return;
+    const long long i = t / k, p = t % k;   // src [m][k] row-major, read coalesced
+    dst[p * C + slots[i]] = (R)src[t];
+}
+
+template <typename R>
+__global__ void gather_cols_kernel(const R* __restrict__ src, double* __restrict__ dst, const int* __restrict__ slots,
+                                   int m, int k, long long C, double scale) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m * k) return;
+    const long long i = t / k, p = t % k;
+    dst[t] = (double)src[p * C + slots[i]] * scale;
+}
+
+template <typename T>
+__global__ void scatter_scalar_kernel(const T* __restrict__ src, T* __restrict__ dst, const int* __restrict__ slots,
+                                      int m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) dst[slots[i]] = src[i];
+}
+
+cudaError_t launch_scatter_cols(const double* src, void* dst, const int* slots, int m, int k, long long C, bool f32,
+                                cudaStream_t st) {
+    const long long total = (long long)m * k;
+    if (total == 0) return cudaSuccess;
+    if (f32) scatter_cols_kernel<float><<<blocks_for(total), 256, 0, st>>>(src, (float*)dst, slots, m, k, C);
+    else scatter_cols_kernel<double><<<blocks_for(total), 256, 0, st>>>(src, (double*)dst, slots, m, k, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_cols(const void* src, double* dst, const int* slots, int m, int k, long long C, bool f32,
+                               double scale, cudaStream_t st) {
+    const long long total = (long long)m * k;
+    if (total == 0) return cudaSuccess;
+    if (f32) gather_cols_kernel<float><<<blocks_for(total), 256, 0, st>>>((const float*)src, dst, slots, m, k, C, scale);
+    else gather_cols_kernel<double><<<blocks_for(total), 256, 0, st>>>((const double*)src, dst, slots, m, k, C, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_u32(const unsigned* src, unsigned* dst, const int* slots, int m, cudaStream_t st) {
+    if (m == 0) return cudaSuccess;
+    scatter_scalar_kernel<unsigned><<<(m + 255) / 256, 256, 0, st>>>(src, dst, slots, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_i32(const int* src, int* dst, const int* slots, int m, cudaStream_t st) {
+    if (m == 0) return cudaSuccess;
+    scatter_scalar_kernel<int><<<(m + 255) / 256, 256, 0, st>>>(src, dst, slots, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_i64(const long long* src, long long* dst, const int* slots, int m, cudaStream_t st) {
+    if (m == 0) return cudaSuccess;
+    scatter_scalar_kernel<long long><<<(m + 255) / 256, 256, 0, st>>>(src, dst, slots, m);
+    return cudaGetLastError();
+}
+
+}  // namespace pk

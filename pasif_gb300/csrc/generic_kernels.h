@@ -19,6 +19,15 @@ cudaError_t launch_from_interleaved(const void* src, double* dst, int B, int k, 
                                     double scale = 1.0);
 // Measured FMA throughput of this GPU (FLOP/s, FMA = 2) in FP32 or FP64.
 cudaError_t measure_fma_peak(bool f32, double* flops_per_s);
+// Serving pools: src[m][k] double -> dst[k][C] columns slots[i]; the inverse
+// gather (scaled); per-slot scalar scatters.
+cudaError_t launch_scatter_cols(const double* src, void* dst, const int* slots, int m, int k, long long C, bool f32,
+                                cudaStream_t st);
+cudaError_t launch_gather_cols(const void* src, double* dst, const int* slots, int m, int k, long long C, bool f32,
+                               double scale, cudaStream_t st);
+cudaError_t launch_scatter_u32(const unsigned* src, unsigned* dst, const int* slots, int m, cudaStream_t st);
+cudaError_t launch_scatter_i32(const int* src, int* dst, const int* slots, int m, cudaStream_t st);
+cudaError_t launch_scatter_i64(const long long* src, long long* dst, const int* slots, int m, cudaStream_t st);
 // element-wise double -> compute precision
 cudaError_t launch_convert(const double* src, void* dst, long long n, bool f32, cudaStream_t st);
 

@@ -347,6 +347,43 @@ std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsign
     return o.str();
 }
 
+std::string pool_source(const Pattern& pat, const FwdKernelKey& key) {
+    Literals none;   // a pool's slots change owner: every value is loaded
+    Emitter em(pat, none);
+    std::ostringstream o;
+    o << "// generated by pasif_gb300 jit.cpp: serving pool chunk, n=" << pat.n << " P=" << pat.P() << "\n";
+    emit_sys_head(o, pat, em, key.f32);
+    o << "};\n";
+    const int W = key.window;
+    o << "struct JW {\n  static constexpr int W = " << W << ";\n";
+    for (int which = 0; which < 2; ++which) {
+        o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";
+        const std::vector<double>& wv = which ? key.wc : key.wn;
+        for (int i = 0; i < W; ++i) o << "i == " << i << " ? " << hexlit(wv[i]) << " : ";
+        o << "R(0); }\n";
+    }
+    o << "};\n}  // namespace pk\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(" << key.block << ") pk_pool(pk::PoolArgs<pk::R> p) {\n";
+    o << "  using namespace pk;\n";
+    o << "  const int b = blockIdx.x * blockDim.x + threadIdx.x;\n";
+    o << "  if (b >= p.C) return;\n";
+    o << "  if (p.remain[b] <= 0) return;\n";
+    o << "  JSys sys;\n  sys.load(p.vals, (long long)p.C, b);\n";
+    o << "  pool_run_iv<R, " << pat.n << ", " << (key.kahan ? "true" : "false") << ", "
+      << (key.max_mask ? "true" : "false") << ", " << (key.sq_mask ? "true" : "false") << ", JW>(sys, p, b, "
+      << key.max_mask << "ull, " << key.sq_mask << "ull);\n";
+    o << "}\n";
+    return o.str();
+}
+
+bool get_pool_kernel(const Pattern& pat, const FwdKernelKey& key, JitKernel* out, std::string* err) {
+    if (pat.n <= 0 || pat.n > kJitMaxN) {
+        *err = "state size outside the specialised range";
+        return false;
+    }
+    return get_cached(pool_source(pat, key), "pk_pool", key.block, out, err);
+}
+
 bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, JitKernel* out,
                     std::string* err) {
     if (pat.n <= 0 || pat.n > kJitMaxN || pat.P() > 1024) {

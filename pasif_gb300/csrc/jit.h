@@ -47,6 +47,9 @@ bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey&
 std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask);
 bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, JitKernel* out,
                     std::string* err);
+// Serving-pool chunk kernel (PoolArgs): values always loaded, no literals.
+std::string pool_source(const Pattern& pat, const FwdKernelKey& key);
+bool get_pool_kernel(const Pattern& pat, const FwdKernelKey& key, JitKernel* out, std::string* err);
 // Compile a source without loading it (no GPU needed); report = compiler log.
 bool compile_report(const std::string& src, std::string* report, std::string* err);
 
@@ -56,6 +59,6 @@ bool fwd_compile_report(const Pattern& pat, const Literals& lit, const FwdKernel
                         std::string* err);
 
 // Largest state size the register-resident specialisation accepts.
-constexpr int kJitMaxN = 64;
+constexpr int kJitMaxN = 128;
 
 }  // namespace pasif

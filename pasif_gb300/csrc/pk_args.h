@@ -55,6 +55,29 @@ struct FwdArgs {
     unsigned long long sq_mask;    // components reduced by sum q^2
 };
 
+// Serving pool: C slots of one pattern, each slot an instance of some request
+// at its own step index; one launch advances every busy slot by `chunk` steps.
+template <typename R>
+struct PoolArgs {
+    const R* vals;              // [P][C]
+    R* state;                   // [n][C]
+    R* comp;                    // [n][C] Kahan compensation, carried between chunks
+    R* mx;                      // [n][C] running max |q|
+    R* sq;                      // [C] running sum q^2
+    R* sqc;                     // [C] its compensation
+    unsigned* step;             // [C] next step index
+    int* remain;                // [C] steps left (<= 0: free slot)
+    const long long* ebase;     // [C] first sample of the slot's signal row in the arena
+    const long long* lim;       // [C] end of the slot's request table in the arena
+    const unsigned* len;        // [C] signal length of the slot's request
+    const int* max_start;       // [C]
+    const int* sq_start;        // [C]
+    Forcing<R> frc;             // x = the signal arena (len / total per slot)
+    R h, h2, h6;
+    int C;
+    int chunk;
+};
+
 // Exact discrete adjoint of the RK4 map with sqrt(N) checkpoints.
 template <typename R>
 struct AdjArgs {

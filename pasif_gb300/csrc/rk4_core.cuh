@@ -324,23 +324,31 @@ __device__ __forceinline__ R sample_at(const Forcing<R>& f, long long idx) {
 // registers and the next one is loaded an interval ahead.  Every forcing
 // value equals force_at's (same operations on the same operands); steps
 // before the first and after the last whole interval use force_at.
+//
+// fwd_core_iv runs rc.nsteps steps from rc.step0 on state already in
+// registers (Q, Kahan compensation Cm, reducers Mx / sq / sqc): the batch
+// kernel calls it once per horizon, the serving pool once per chunk with the
+// state carried in device memory between chunks, which gives the same bits
+// as an uninterrupted run.
+struct RunCtx {
+    long long ebase;     // first sample of this instance's signal row
+    unsigned step0;
+    unsigned nsteps;
+    int max_start;
+    int sq_start;
+};
+
 template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, class WP, class Sys, class V>
-__device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, int b,
-                                           unsigned long long max_mask, unsigned long long sq_mask,
-                                           V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx) {
+__device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a, const Forcing<R>& frc, int b,
+                                            const RunCtx& rc, unsigned long long max_mask,
+                                            unsigned long long sq_mask, V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx,
+                                            R& sq, R& sqc) {
     typedef M<R> m;
     constexpr int W = WP::W;
     constexpr unsigned SPI = W == 0 ? 1u : (unsigned)(W / 2);
     const long long B = a.B;
-    const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
-    const unsigned len = a.frc.len;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        Q[i] = a.state[i * B + b];
-        if (KAHAN) Cm[i] = R(0);
-        if (HMAX) Mx[i] = R(0);
-    }
-    R sq = R(0), sqc = R(0);
+    const long long ebase = rc.ebase;
+    const unsigned len = frc.len;
     auto post = [&](unsigned step) {
         if (HTRAJ && step % (unsigned)a.traj_every == 0u) {
             const long long slot = (long long)(step / (unsigned)a.traj_every) -
@@ -351,12 +359,12 @@ __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, 
                 for (int i = 0; i < N; ++i) a.traj[(slot * N + i) * B + b] = Q[i];
             }
         }
-        if (HMAX && (long long)step >= (long long)a.max_start) {
+        if (HMAX && (long long)step >= (long long)rc.max_start) {
 #pragma unroll
             for (int i = 0; i < N; ++i)
                 if (i < 64 && ((max_mask >> i) & 1ull)) Mx[i] = m::max(Mx[i], m::abs(Q[i]));
         }
-        if (HSQ && (long long)step >= (long long)a.sq_start) {
+        if (HSQ && (long long)step >= (long long)rc.sq_start) {
 #pragma unroll
             for (int i = 0; i < N; ++i)
                 if (i < 64 && ((sq_mask >> i) & 1ull)) {
@@ -372,20 +380,19 @@ __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, 
                 }
         }
     };
-    unsigned s = a.step0;
-    const unsigned end = a.step0 + (unsigned)a.nsteps;
+    unsigned s = rc.step0;
+    const unsigned end = rc.step0 + rc.nsteps;
     while (s < end && (s % SPI) != 0u) {
-        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, force_at(a.frc, ebase, s, 0u, 0u),
-                              force_at(a.frc, ebase, s, 0u, 1u), force_at(a.frc, ebase, s, 1u, 0u), a.h, a.h2,
-                              a.h6);
+        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u), force_at(frc, ebase, s, 0u, 1u),
+                              force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6);
         post(s);
         ++s;
     }
     if (end - s >= SPI) {
         unsigned j = s / SPI;
-        R x0 = sample_at(a.frc, ebase + j), x1 = sample_at(a.frc, ebase + j + 1), x2 = sample_at(a.frc, ebase + j + 2);
+        R x0 = sample_at(frc, ebase + j), x1 = sample_at(frc, ebase + j + 1), x2 = sample_at(frc, ebase + j + 2);
         for (; end - s >= SPI; s += SPI, ++j) {
-            const R nxt = sample_at(a.frc, ebase + j + 3);
+            const R nxt = sample_at(frc, ebase + j + 3);
             const bool g0 = j > 0u && j < len;
             const bool g1 = j + 1u > 0u && j + 1u < len;
             R uc;
@@ -413,12 +420,35 @@ __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, 
         }
     }
     while (s < end) {
-        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, force_at(a.frc, ebase, s, 0u, 0u),
-                              force_at(a.frc, ebase, s, 0u, 1u), force_at(a.frc, ebase, s, 1u, 0u), a.h, a.h2,
-                              a.h6);
+        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u), force_at(frc, ebase, s, 0u, 1u),
+                              force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6);
         post(s);
         ++s;
     }
+}
+
+// One batch instance over the whole horizon (initial state in a.state, final
+// state and reducers out).
+template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, class WP, class Sys, class V>
+__device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, int b,
+                                           unsigned long long max_mask, unsigned long long sq_mask,
+                                           V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx) {
+    const long long B = a.B;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        Q[i] = a.state[i * B + b];
+        if (KAHAN) Cm[i] = R(0);
+        if (HMAX) Mx[i] = R(0);
+    }
+    R sq = R(0), sqc = R(0);
+    RunCtx rc;
+    rc.ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+    rc.step0 = a.step0;
+    rc.nsteps = (unsigned)a.nsteps;
+    rc.max_start = a.max_start;
+    rc.sq_start = a.sq_start;
+    fwd_core_iv<R, N, KAHAN, HMAX, HSQ, HTRAJ, WP>(sys, a, a.frc, b, rc, max_mask, sq_mask, Q, Cm, S, K, Mi, Mx, sq,
+                                                   sqc);
 #pragma unroll
     for (int i = 0; i < N; ++i) a.state[i * B + b] = Q[i];
     if (HMAX) {
@@ -428,6 +458,53 @@ __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, 
             if (i < 64 && ((max_mask >> i) & 1ull)) { a.out_max[slot * B + b] = Mx[i]; ++slot; }
     }
     if (HSQ) a.out_sq[b] = sq;
+}
+
+// Serving pool: slot b advances min(chunk, remaining) steps from its own step
+// index, its state, Kahan compensation and reducers carried in device memory
+// (PoolArgs, pk_args.h).  Free slots (remaining <= 0) return at once.
+template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, class WP, class Sys>
+__device__ __forceinline__ void pool_run_iv(const Sys& sys, const PoolArgs<R>& p, int b,
+                                            unsigned long long max_mask, unsigned long long sq_mask) {
+    const int rem = p.remain[b];
+    if (rem <= 0) return;
+    const long long C = p.C;
+    RegVec<R, N> Q, Cm, S, K, Mi, Mx;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        Q[i] = p.state[i * C + b];
+        if (KAHAN) Cm[i] = p.comp[i * C + b];
+        if (HMAX) Mx[i] = p.mx[i * C + b];
+    }
+    R sq = HSQ ? p.sq[b] : R(0), sqc = HSQ ? p.sqc[b] : R(0);
+    FwdArgs<R> a;   // the fields fwd_core_iv reads: B, h, h2, h6 (no trajectory)
+    a.B = p.C;
+    a.h = p.h;
+    a.h2 = p.h2;
+    a.h6 = p.h6;
+    a.traj = nullptr;
+    a.traj_every = 1;
+    a.traj_slots = 0;
+    a.step0 = 0;
+    Forcing<R> frc = p.frc;
+    frc.len = p.len[b];
+    frc.total = p.lim[b];
+    RunCtx rc;
+    rc.ebase = p.ebase[b];
+    rc.step0 = p.step[b];
+    rc.nsteps = (unsigned)(rem < p.chunk ? rem : p.chunk);
+    rc.max_start = p.max_start[b];
+    rc.sq_start = p.sq_start[b];
+    fwd_core_iv<R, N, KAHAN, HMAX, HSQ, false, WP>(sys, a, frc, b, rc, max_mask, sq_mask, Q, Cm, S, K, Mi, Mx, sq, sqc);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        p.state[i * C + b] = Q[i];
+        if (KAHAN) p.comp[i * C + b] = Cm[i];
+        if (HMAX) p.mx[i * C + b] = Mx[i];
+    }
+    if (HSQ) { p.sq[b] = sq; p.sqc[b] = sqc; }
+    p.step[b] = rc.step0 + rc.nsteps;
+    p.remain[b] = rem - (int)rc.nsteps;
 }
 
 // Exact discrete adjoint for pattern-specialised kernels: the same algorithm

@@ -167,12 +167,13 @@ def coupled2(n_sys: int = 16384, nsteps: int = 200_000, seed: int = 2, n_sig: in
                     notes={"output": "sqrt(p(T)/T), p' = x2^2 (state 4)", "T": nsteps * h})
 
 
-def chain8(n_sys: int = 4096, nsteps: int = 50_000, seed: int = 3) -> Workload:
+def chain8(n_sys: int = 4096, nsteps: int = 50_000, seed: int = 3, nd: int = 8) -> Workload:
     """Config 3: 8-DOF spring chain, tridiagonal K, restoring cubic, 4
     quadratic couplings, sine forcing on DOF 1; loss = h sum of squared
-    positions over the final half (sum-of-squares reducer)."""
+    positions over the final half (sum-of-squares reducer).  `nd` gives the
+    same chain with another number of DOFs (quadratic couplings on every
+    second link)."""
     rng = np.random.default_rng(seed)
-    nd = 8
     n = 2 * nd
     b = _Builder(n)
     cols = []
@@ -191,8 +192,8 @@ def chain8(n_sys: int = 4096, nsteps: int = 50_000, seed: int = 3) -> Workload:
             b.k.append((nd + i, i + 1))
             cols.append(-off[:, i])
     kv = np.stack(cols, axis=1)
-    b.g = [(nd + i, i, i + 1) for i in (0, 2, 4, 6)]
-    gv = rng.normal(0.0, 0.2, (n_sys, 4))
+    b.g = [(nd + i, i, i + 1) for i in range(0, nd - 1, 2)]
+    gv = rng.normal(0.0, 0.2, (n_sys, len(b.g)))
     b.l = [(nd + i, i, i, i) for i in range(nd)]
     lv = -rng.uniform(0.0, 2.0, (n_sys, nd))
     b.f = [nd]
@@ -202,8 +203,8 @@ def chain8(n_sys: int = 4096, nsteps: int = 50_000, seed: int = 3) -> Workload:
     h = 1e-3
     t = np.arange(nsteps + 2) * h
     sig = np.sin(2 * np.pi * f[:, None] * t[None, :])
-    return Workload("chain_8dof_adjoint", pat, vals, np.zeros((n_sys, n)), np.arange(n_sys, dtype=np.int32), sig, 2,
-                    linear_weights(2), h, nsteps, 1000, sq_comp=tuple(range(nd)), sq_start=nsteps // 2,
+    return Workload(f"chain_{nd}dof_adjoint", pat, vals, np.zeros((n_sys, n)), np.arange(n_sys, dtype=np.int32), sig,
+                    2, linear_weights(2), h, nsteps, 1000, sq_comp=tuple(range(min(nd, 64))), sq_start=nsteps // 2,
                     notes={"loss": "h * sum_{s >= N/2} sum_i x_i(s+1)^2"})
 
 
@@ -265,3 +266,95 @@ def banded32(n_sys: int = 2048, nsteps: int = 1_000_000, seed: int = 4, n_sig: i
 
 
 CONFIGS = {"duffing": duffing, "coupled2": coupled2, "chain8": chain8, "banded32": banded32}
+
+
+# ---- served mixed stream (config 5) -----------------------------------------
+
+SERVED_DOFS = (1, 2, 4, 8, 16, 32, 64)
+
+
+@dataclass
+class ServedClass:
+    """One request class of the served stream: a pattern with its time step
+    and forcing interpolation; `positions` are the displacement components
+    (amplitudes of a forward sweep, loss of an adjoint sweep)."""
+    dof: int
+    pattern: Pattern
+    h: float
+    window: int
+    im: np.ndarray
+    positions: tuple
+    family: str
+
+    def sample(self, n_sys: int, seed: int) -> np.ndarray:
+        """values[n_sys][P] drawn as by the family's generator."""
+        if self.family == "duffing":
+            return duffing(n_sys=n_sys, nsteps=10, seed=seed).values
+        if self.family == "coupled2":
+            return coupled2(n_sys=n_sys, nsteps=10, seed=seed, sig_len=64).values
+        if self.family == "banded32":
+            return banded32(n_sys=n_sys, nsteps=10, seed=seed, sig_len=64).values
+        return chain8(n_sys=n_sys, nsteps=10, seed=seed, nd=self.dof).values
+
+
+def served_class(dof: int) -> ServedClass:
+    """Request class with `dof` degrees of freedom: the Duffing oscillator
+    (1), the coupled pair (2), the banded system (32) and the spring chain of
+    that length otherwise."""
+    if dof == 1:
+        w = duffing(n_sys=1, nsteps=10)
+        return ServedClass(1, w.pattern, 1e-4, 2, linear_weights(2), (0,), "duffing")
+    if dof == 2:
+        w = coupled2(n_sys=1, nsteps=10, sig_len=64)
+        return ServedClass(2, w.pattern, 1e-3, 8, linear_weights(8), (0, 1), "coupled2")
+    if dof == 32:
+        w = banded32(n_sys=1, nsteps=10, sig_len=64)
+        return ServedClass(32, w.pattern, 5e-4, 2, linear_weights(2), tuple(range(32)), "banded32")
+    w = chain8(n_sys=1, nsteps=10, nd=dof)
+    return ServedClass(dof, w.pattern, 1e-3, 2, linear_weights(2), tuple(range(min(dof, 64))), "chain")
+
+
+@dataclass
+class ServedRequest:
+    rid: int
+    kind: str              # "forward" or "adjoint"
+    dof: int
+    arrival: float         # seconds after the start of the stream
+    n_sys: int
+    nsteps: int
+    seed: int
+
+
+def served_stream(rate: float = 200.0, duration: float = 1.0, seed: int = 5, max_systems: int = 4096,
+                  min_steps: int = 10_000, max_steps: int = 200_000, adjoint_fraction: float = 0.3,
+                  dofs=SERVED_DOFS):
+    """Poisson arrivals at `rate` per second for `duration` seconds: forward or
+    adjoint (70/30) sweeps of log-uniform 1..max_systems systems of a DOF drawn
+    from `dofs`, log-uniform min_steps..max_steps RK4 steps."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        n = int(np.exp(rng.uniform(0.0, np.log(max_systems))))
+        steps = int(np.exp(rng.uniform(np.log(min_steps), np.log(max_steps))))
+        kind = "adjoint" if rng.random() < adjoint_fraction else "forward"
+        out.append(ServedRequest(len(out), kind, int(rng.choice(dofs)), t, max(1, n), steps,
+                                 int(rng.integers(1 << 30))))
+    return out
+
+
+def served_signals(seed: int, nsteps: int, window: int, h: float, rows: int = 4) -> np.ndarray:
+    """`rows` random-phase multisines long enough for nsteps steps (one sample
+    per window/2 steps, float32 values)."""
+    rng = np.random.default_rng(seed)
+    spacing = max(1, window // 2)
+    length = nsteps // spacing + 3
+    t = np.arange(length) * h * spacing
+    sig = np.zeros((rows, length))
+    for r in range(rows):
+        fr = rng.uniform(0.05, 1.0, 4)
+        ph = rng.uniform(0.0, 2 * np.pi, 4)
+        sig[r] = np.sin(2 * np.pi * fr[:, None] * t[None, :] + ph[:, None]).sum(axis=0) / 2.0
+    return sig.astype(np.float32).astype(np.float64)

@@ -44,6 +44,117 @@ static std::vector<T> readf(const char* dir, const char* name, size_t n) {
     return v;
 }
 
+#ifdef EMU_POOL
+// Serving pool: C slots, jobs admitted into given slots before given chunks,
+// harvested after the chunk in which their slot ran out of steps.
+// argv: dir C n P S W chunk h n_jobs n_chunks
+// jobs.bin: int64 [J][8] = slot, admit_chunk, nsteps, ebase, lim, len, max_start, sq_start
+// vals.bin [J][P], x0.bin [J][n], arena.bin [S], im.bin [2W] (compute precision)
+// out: state.bin [J][n], mx.bin [J][n], sq.bin [J], done.bin int32 [J] (chunk of harvest)
+int main(int argc, char** argv) {
+    if (argc < 11) return 1;
+    const char* dir = argv[1];
+    const int C = std::atoi(argv[2]), n = std::atoi(argv[3]), P = std::atoi(argv[4]);
+    const long long S = std::atoll(argv[5]);
+    const int W = std::atoi(argv[6]), chunk = std::atoi(argv[7]);
+    const double h = std::atof(argv[8]);
+    const int J = std::atoi(argv[9]), T = std::atoi(argv[10]);
+    typedef pk::R R;
+    auto jobs = readf<long long>(dir, "jobs.bin", (size_t)J * 8);
+    auto jv = readf<R>(dir, "vals.bin", (size_t)J * P);
+    auto jx = readf<R>(dir, "x0.bin", (size_t)J * n);
+    auto arena = readf<R>(dir, "arena.bin", (size_t)S);
+    auto im = readf<R>(dir, "im.bin", (size_t)2 * W);
+    std::vector<R> vals((size_t)(P > 0 ? P : 1) * C, R(0)), state((size_t)n * C, R(0)), comp((size_t)n * C, R(0)),
+        mx((size_t)n * C, R(0)), sq(C, R(0)), sqc(C, R(0));
+    std::vector<unsigned> step(C, 0u), len(C, 0u);
+    std::vector<int> remain(C, 0), mstart(C, 0), sstart(C, 0), owner(C, -1), done(J, -1);
+    std::vector<long long> ebase(C, 0), lim(C, 0);
+    std::vector<R> os((size_t)J * n, R(0)), om((size_t)J * n, R(0)), oq(J, R(0));
+    pk::PoolArgs<R> p;
+    std::memset(&p, 0, sizeof p);
+    p.vals = vals.data();
+    p.state = state.data();
+    p.comp = comp.data();
+    p.mx = mx.data();
+    p.sq = sq.data();
+    p.sqc = sqc.data();
+    p.step = step.data();
+    p.remain = remain.data();
+    p.ebase = ebase.data();
+    p.lim = lim.data();
+    p.len = len.data();
+    p.max_start = mstart.data();
+    p.sq_start = sstart.data();
+    p.frc.x = arena.data();
+    p.frc.im = W ? im.data() : nullptr;
+    p.frc.total = S;
+    p.frc.w = (unsigned)W;
+    while (W && (1u << p.frc.lw) < (unsigned)W) p.frc.lw++;
+    p.h = (R)h;
+    p.h2 = (R)(h / 2.0);
+    p.h6 = (R)(h / 6.0);
+    p.C = C;
+    p.chunk = chunk;
+    blockDim.x = 128;
+    auto harvest = [&](int c) {
+        for (int b = 0; b < C; ++b) {
+            const int j = owner[b];
+            if (j < 0 || remain[b] > 0) continue;
+            for (int i = 0; i < n; ++i) {
+                os[(size_t)j * n + i] = state[(size_t)i * C + b];
+                om[(size_t)j * n + i] = mx[(size_t)i * C + b];
+            }
+            oq[j] = sq[b];
+            done[j] = c;
+            owner[b] = -1;
+        }
+    };
+    for (int c = 0; c <= T; ++c) {
+        harvest(c);
+        if (c == T) break;
+        for (int j = 0; j < J; ++j) {
+            const long long* q = &jobs[(size_t)j * 8];
+            if (q[1] != c) continue;
+            const int b = (int)q[0];
+            if (b < 0 || b >= C || owner[b] >= 0) { std::fprintf(stderr, "slot %d busy\n", b); return 3; }
+            owner[b] = j;
+            for (int k = 0; k < P; ++k) vals[(size_t)k * C + b] = jv[(size_t)j * P + k];
+            for (int i = 0; i < n; ++i) {
+                state[(size_t)i * C + b] = jx[(size_t)j * n + i];
+                comp[(size_t)i * C + b] = R(0);
+                mx[(size_t)i * C + b] = R(0);
+            }
+            sq[b] = sqc[b] = R(0);
+            step[b] = 0u;
+            remain[b] = (int)q[2];
+            ebase[b] = q[3];
+            lim[b] = q[4];
+            len[b] = (unsigned)q[5];
+            mstart[b] = (int)q[6];
+            sstart[b] = (int)q[7];
+        }
+        for (int b = 0; b < C; ++b) {
+            blockIdx.x = (unsigned)(b / 128);
+            threadIdx.x = (unsigned)(b % 128);
+            pk_pool(p);
+        }
+    }
+    for (int j = 0; j < J; ++j)
+        if (done[j] < 0) { std::fprintf(stderr, "job %d unfinished\n", j); return 4; }
+    char path[1024];
+    const struct { const char* name; const void* p; size_t bytes; } outs[] = {
+        {"state.bin", os.data(), os.size() * sizeof(R)}, {"mx.bin", om.data(), om.size() * sizeof(R)},
+        {"sq.bin", oq.data(), oq.size() * sizeof(R)}, {"done.bin", done.data(), done.size() * sizeof(int)}};
+    for (const auto& o : outs) {
+        std::snprintf(path, sizeof path, "%s/%s", dir, o.name);
+        FILE* f = std::fopen(path, "wb");
+        std::fwrite(o.p, 1, o.bytes, f);
+        std::fclose(f);
+    }
+    return 0;
+}
+#else
 // argv: dir B n P n_exc len window step0 nsteps h kahan
 int main(int argc, char** argv) {
     if (argc < 12) return 1;
@@ -139,3 +250,4 @@ int main(int argc, char** argv) {
 #endif
     return 0;
 }
+#endif

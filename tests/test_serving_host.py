@@ -1,0 +1,162 @@
+"""Host logic of the serving loop, driven with fake pools and a fake adjoint
+runner (no GPU): first-come-first-served admission by free slots and arena
+space, refusal of requests that can never fit, the adjoint memory budget,
+and latency bookkeeping."""
+import threading
+
+import numpy as np
+import pytest
+
+from pasif_gb300 import serving as S
+from pasif_gb300.system import Pattern
+
+PAT = Pattern.from_dense_lists(2, [0, 1], [1, 0], (), (), (), [1])[0]
+
+
+class FakePool:
+    """Slots and arena like pasif_pool: admit fails when either is short;
+    launch advances every request by `chunk` steps."""
+
+    def __init__(self, capacity, arena, chunk, log):
+        self.capacity, self.arena, self.chunk = capacity, arena, chunk
+        self.free, self.used_arena = capacity, 0
+        self.reqs, self.next, self.log = {}, 1, log
+
+    def admit(self, values, x0, exc_index, signals, nsteps, max_start=0, sq_start=0):
+        m, t = len(values), np.asarray(signals).size
+        if m > self.free or t > self.arena - self.used_arena:
+            return None
+        rid, self.next = self.next, self.next + 1
+        self.free -= m
+        self.used_arena += t
+        self.reqs[rid] = [nsteps, m, t, np.asarray(values)]
+        self.log.append(("admit", rid, self.capacity - self.free))
+        return rid
+
+    def launch(self):
+        for r in self.reqs.values():
+            r[0] -= self.chunk
+
+    def poll(self):
+        return [rid for rid, r in self.reqs.items() if r[0] <= 0]
+
+    def harvest(self, rid, n_sys):
+        _, m, t, v = self.reqs.pop(rid)
+        self.free += m
+        self.used_arena -= t
+        return v[:, :2] * 2.0, v[:, :1], v[:, 0]
+
+
+def make_server(capacity=8, arena=1000, budget=100, workers=2, runner=None, log=None):
+    log = [] if log is None else log
+    spec = S.ClassSpec(PAT, 0.01, 0, None, (0,), chunk=10)
+    return S.Server({"a": spec}, capacity=capacity, arena_samples=arena, adjoint_budget=budget,
+                    adjoint_workers=workers, pool_factory=lambda sp: FakePool(capacity, arena, sp.chunk, log),
+                    adjoint_runner=runner or (lambda sp, rq, st: (rq.values * 3.0, rq.x0)),
+                    stream_factory=lambda: None), log
+
+
+def req(rid, kind, n, nsteps=25, table=10):
+    return S.Request(rid, kind, "a", np.full((n, PAT.P), float(rid)), np.zeros((n, 2)), np.zeros(n, np.int32),
+                     np.zeros((1, table)), nsteps)
+
+
+def test_forward_admission_and_results():
+    srv, log = make_server()
+    srv.start()
+    for i, n in enumerate([6, 6, 3, 8, 9]):
+        srv.submit(req(i, "forward", n))
+    assert srv.wait(10.0)
+    srv.stop()
+    res = srv.results()
+    assert res[4].error and "larger than a serving pool" in res[4].error
+    for i, n in enumerate([6, 6, 3, 8]):
+        assert res[i].error is None
+        np.testing.assert_array_equal(res[i].state, np.full((n, 2), 2.0 * i))
+        assert res[i].t_arrival <= res[i].t_admit <= res[i].t_done
+    assert max(busy for _, _, busy in log) <= 8          # never more slots than the pool has
+    order = [rid for ev, rid, _ in log if ev == "admit"]
+    assert order == sorted(order)                       # first come, first served
+
+
+def test_arena_limits_admission():
+    srv, log = make_server(capacity=64, arena=25)
+    srv.start()
+    for i in range(4):
+        srv.submit(req(i, "forward", 1, table=10))      # two tables fit at a time
+    srv.submit(req(9, "forward", 1, table=26))           # never fits
+    assert srv.wait(10.0)
+    srv.stop()
+    res = srv.results()
+    assert res[9].error is not None
+    assert all(res[i].error is None for i in range(4))
+
+
+def test_adjoint_budget():
+    lock, state = threading.Lock(), {"now": 0, "peak": 0}
+    need = S.adjoint_bytes(PAT, 4, 25, 10, "fp32_kahan")
+
+    def runner(spec, rq, stream):
+        with lock:
+            state["now"] += need
+            state["peak"] = max(state["peak"], state["now"])
+        threading.Event().wait(0.02)
+        with lock:
+            state["now"] -= need
+        return rq.values * 3.0, rq.x0
+
+    srv, _ = make_server(budget=need + need // 2, workers=3, runner=runner)   # one adjoint at a time
+    srv.start()
+    for i in range(4):
+        srv.submit(req(i, "adjoint", 4))
+    srv.submit(req(7, "adjoint", 400))                   # larger than the whole budget
+    assert srv.wait(10.0)
+    srv.stop()
+    res = srv.results()
+    assert res[7].error is not None and "budget" in res[7].error
+    for i in range(4):
+        assert res[i].error is None
+        np.testing.assert_array_equal(res[i].d_values, np.full((4, PAT.P), 3.0 * i))
+    assert state["peak"] == need
+
+
+def test_adjoint_errors():
+    """A request whose solve returns an error status gets an error result and
+    the worker serves the next; any other exception stops the server and is
+    raised by wait()."""
+    from pasif_gb300 import _native as N
+
+    def runner(spec, rq, stream):
+        if rq.rid == 0:
+            raise N.PasifError(N.ERR_INVALID, "bad request")
+        if rq.rid == 2:
+            raise RuntimeError("boom")
+        return rq.values, rq.x0
+
+    srv, _ = make_server(budget=1 << 30, workers=1, runner=runner)
+    srv.start()
+    srv.submit(req(0, "adjoint", 1))
+    srv.submit(req(1, "adjoint", 1))
+    assert srv.wait(10.0)
+    res = srv.results()
+    assert "bad request" in res[0].error and res[1].error is None
+    srv.submit(req(2, "adjoint", 1))
+    with pytest.raises(RuntimeError, match="boom"):
+        srv.wait(10.0)
+    srv.stop()
+
+
+def test_percentile():
+    assert S.percentile([3.0, 1.0, 2.0], 50) == 2.0
+    assert S.percentile([1.0, 2.0], 99) == pytest.approx(1.99)
+
+
+def test_served_stream_shape():
+    from pasif_gb300 import synth
+    st = synth.served_stream(rate=200.0, duration=2.0, seed=1)
+    assert 300 < len(st) < 500
+    assert all(1 <= r.n_sys <= 4096 and 10_000 <= r.nsteps <= 200_000 for r in st)
+    assert all(a.arrival < b.arrival for a, b in zip(st, st[1:]))
+    frac = sum(r.kind == "adjoint" for r in st) / len(st)
+    assert 0.2 < frac < 0.4
+    assert {r.dof for r in st} == set(synth.SERVED_DOFS)

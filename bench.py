@@ -29,6 +29,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# the served stream runs a pool per request class and a stream per adjoint
+# worker: enough hardware queues that they do not serialise (read at CUDA init)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "RK4 system-steps/s (FP32 vs FP64 @<=1e-5 rel err); adjoint grads/s; p99 ms"
 UNIT = "system-steps/s"

@@ -49,6 +49,10 @@ extern "C" {
 #define PASIF_PLAN_NO_LITERALS 2    /* plan flag: specialise to the pattern
                                        only, load every value (one compiled
                                        kernel serves all batches of a plan) */
+#define PASIF_PLAN_WARP_SLICED 4    /* plan flag: warp-sliced kernels at any
+                                       size (default: from n >= 28 in FP32,
+                                       n >= 24 in FP64)                     */
+#define PASIF_PLAN_NO_WARP_SLICED 8 /* plan flag: thread per system always  */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* pasif_last_error(void);
@@ -175,7 +179,7 @@ typedef struct pasif_batch pasif_batch;
 
 /* Plan = pattern + precision (the pattern-specialised kernels are compiled
  * lazily, per batch, by the first solve).  flags: PASIF_PLAN_GENERIC_ONLY,
- * PASIF_PLAN_NO_LITERALS. */
+ * PASIF_PLAN_NO_LITERALS, PASIF_PLAN_WARP_SLICED, PASIF_PLAN_NO_WARP_SLICED. */
 int pasif_plan_create(pasif_plan** out, const pasif_pattern* pattern, int precision, int flags);
 int pasif_plan_destroy(pasif_plan* p);
 
@@ -231,7 +235,7 @@ int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys,
 typedef struct pasif_pool pasif_pool;
 int pasif_pool_create(pasif_pool** out, const pasif_pattern* pattern, int precision, int window,
                       const double* im, double h, const pasif_reducers* red, int capacity,
-                      long long arena_samples, int chunk);
+                      long long arena_samples, int chunk, int flags);
 int pasif_pool_destroy(pasif_pool* p);
 /* Host arrays: values[n_sys][P], x0[n_sys][n], exc_index[n_sys],
  * signals[n_exc][len]; integrates nsteps from step 0.  PASIF_ERR_STATE when

@@ -27,6 +27,8 @@ HOST, DEVICE = 0, 1
 KERNEL_NONE, KERNEL_GENERIC, KERNEL_SPECIALISED = 0, 1, 2
 PLAN_GENERIC_ONLY = 1
 PLAN_NO_LITERALS = 2
+PLAN_WARP_SLICED = 4
+PLAN_NO_WARP_SLICED = 8
 
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32_kahan": FP32_KAHAN}
 
@@ -113,7 +115,7 @@ _SIGS = {
     "pasif_plan_jit_report_adjoint": (C.c_int, [_vp, _dp, C.c_int, C.c_ulonglong, C.c_char_p, C.c_longlong, _llp]),
     "pasif_batch_adjoint_kernel": (C.c_int, [_vp, _ip]),
     "pasif_pool_create": (C.c_int, [C.POINTER(_vp), C.POINTER(PatternC), C.c_int, C.c_int, _dp, C.c_double,
-                                    C.POINTER(ReducersC), C.c_int, C.c_longlong, C.c_int]),
+                                    C.POINTER(ReducersC), C.c_int, C.c_longlong, C.c_int, C.c_int]),
     "pasif_pool_destroy": (C.c_int, [_vp]),
     "pasif_pool_admit": (C.c_int, [_vp, C.c_int, _dp, _dp, _ip, _dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    _ip]),

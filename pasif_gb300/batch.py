@@ -29,14 +29,19 @@ def _stream(stream) -> C.c_void_p:
 
 
 class Plan:
-    def __init__(self, pattern: Pattern, precision="fp64", generic_only: bool = False, literals: bool = True):
+    def __init__(self, pattern: Pattern, precision="fp64", generic_only: bool = False, literals: bool = True,
+                 slicing=None):
         """literals=False: the specialised kernels load every value, so one
-        compiled kernel serves every batch of the plan (serving)."""
+        compiled kernel serves every batch of the plan (serving).
+        slicing: None = warp-sliced kernels from n >= 28 (FP32) / 24 (FP64), True = always,
+        False = never (thread per system)."""
         self.pattern = pattern
         self.precision = _prec(precision)
         self._c = pattern.to_c()
         h = C.c_void_p()
         flags = (N.PLAN_GENERIC_ONLY if generic_only else 0) | (0 if literals else N.PLAN_NO_LITERALS)
+        if slicing is not None:
+            flags |= N.PLAN_WARP_SLICED if slicing else N.PLAN_NO_WARP_SLICED
         N.check(N.lib.pasif_plan_create(C.byref(h), C.byref(self._c), self.precision, flags))
         self.handle = h
 

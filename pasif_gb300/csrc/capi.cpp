@@ -309,6 +309,7 @@ int pasif_plan_create(pasif_plan** out, const pasif_pattern* pattern, int precis
         int rc = pasif::plan_create(pat, precision, (flags & PASIF_PLAN_GENERIC_ONLY) != 0, &h->p, &err);
         if (rc) return fail(rc, err);
         h->p->no_literals = (flags & PASIF_PLAN_NO_LITERALS) != 0;
+        h->p->slicing = (flags & PASIF_PLAN_WARP_SLICED) ? 1 : (flags & PASIF_PLAN_NO_WARP_SLICED) ? -1 : 0;
         *out = h.release();
         return PASIF_OK;
     });
@@ -406,7 +407,8 @@ int pasif_batch_kernel_info(pasif_batch* b, int* kind, int* registers) {
 /* ---------------- serving pools ---------------- */
 
 int pasif_pool_create(pasif_pool** out, const pasif_pattern* pattern, int precision, int window, const double* im,
-                      double h, const pasif_reducers* red, int capacity, long long arena_samples, int chunk) {
+                      double h, const pasif_reducers* red, int capacity, long long arena_samples, int chunk,
+                      int flags) {
     return guard([&] {
         if (!out) return fail(PASIF_ERR_INVALID, "null output handle");
         pasif::Pattern pat;
@@ -415,8 +417,9 @@ int pasif_pool_create(pasif_pool** out, const pasif_pattern* pattern, int precis
         pasif::Reducers r;
         if (!to_reducers(red, &r, &err)) return fail(PASIF_ERR_INVALID, err);
         std::unique_ptr<pasif_pool> h_(new pasif_pool());
+        const int slicing = (flags & PASIF_PLAN_WARP_SLICED) ? 1 : (flags & PASIF_PLAN_NO_WARP_SLICED) ? -1 : 0;
         int rc = pasif::Pool::create(pat, precision, window, im, h, r.max_comp, r.sq_comp, capacity, arena_samples,
-                                     chunk, &h_->p, &err);
+                                     chunk, slicing, &h_->p, &err);
         if (rc) return fail(rc, err);
         *out = h_.release();
         return PASIF_OK;
@@ -494,6 +497,7 @@ int pasif_plan_jit_report_pool(const pasif_plan* p, int window, const double* im
         for (int c : r.max_comp) key.max_mask |= 1ull << c;
         for (int c : r.sq_comp) key.sq_mask |= 1ull << c;
         key.window = window;
+        key.slices = p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0);
         for (int i = 0; i < 2 * window; ++i)
             (i < window ? key.wn : key.wc).push_back(f32 ? (double)(float)im[i] : im[i]);
         const std::string src = pasif::pool_source(p->p->pat, key);
@@ -535,7 +539,9 @@ int pasif_plan_jit_report_adjoint(const pasif_plan* p, const double* values, int
     return guard([&] {
         const bool f32 = p->p->precision != pasif::kFP64;
         const std::string src =
-            pasif::adj_source(p->p->pat, literals_of(p->p->pat, f32, values, n_sys), f32, sq_mask);
+            pasif::adj_source(p->p->pat, literals_of(p->p->pat, f32, values, n_sys), f32, sq_mask,
+                              p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0),
+                              p->p->precision == pasif::kFP32Kahan);
         std::string report, err;
         if (!pasif::compile_report(src, &report, &err)) return fail(PASIF_ERR_NVRTC, err);
         report += "\n// ---- source ----\n" + src;
@@ -589,6 +595,7 @@ int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys, 
         key.kahan = p->p->precision == pasif::kFP32Kahan;
         key.max_mask = max_mask;
         key.sq_mask = sq_mask;
+        key.slices = p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0);
         if (window < 0 || (window > 0 && (!im || (window & (window - 1)))))
             return fail(PASIF_ERR_INVALID, "window must be 0 or a power of two with weights");
         key.window = window;

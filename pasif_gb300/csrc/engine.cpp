@@ -296,7 +296,7 @@ int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Re
     if (B == 0) { last_kind = kNone; return 0; }
     PK_CUDA(cudaMemcpyAsync(state.p, x0.p, (size_t)B * n * rs, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
     const bool kahan = plan->precision == kFP32Kahan;
-    if (!plan->generic_only && n <= kJitMaxN) {
+    if (!plan->generic_only && n <= kWsMaxN) {
         FwdKernelKey key;
         key.f32 = f;
         key.kahan = kahan;
@@ -307,21 +307,22 @@ int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Re
         key.window = (int)sig.w;
         key.wn.assign(sig.im_host.begin(), sig.im_host.begin() + sig.w);
         key.wc.assign(sig.im_host.begin() + sig.w, sig.im_host.end());
+        key.slices = plan->slicing < 0 ? 0 : ws_slices(pat, f, plan->slicing > 0);
         JitKernel k;
         std::string jerr;
         if (get_fwd_kernel(pat, lit, key, &k, &jerr)) {
-            dim3 grid((unsigned)((B + k.block - 1) / k.block));
+            dim3 grid((unsigned)((B + k.per_block - 1) / k.per_block));
             cudaError_t e;
             if (f) {
                 pk::FwdArgs<float> a;
                 fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
                 void* args[] = {&a};
-                e = cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, 0, st);
+                e = cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
             } else {
                 pk::FwdArgs<double> a;
                 fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
                 void* args[] = {&a};
-                e = cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, 0, st);
+                e = cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
             }
             PK_CUDA(e, "specialised forward kernel launch");
             last_kind = kSpecialised;
@@ -439,14 +440,16 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     a.sq_mask = g_sq ? sm : 0ull;
     JitKernel jk;
     std::string jerr;
-    const bool jit = !plan->generic_only && get_adj_kernel(pat, lit, f, g_sq ? sm : 0ull, &jk, &jerr);
+    const int slices = plan->slicing < 0 ? 0 : ws_slices(pat, f, plan->slicing > 0);
+    const bool jit = !plan->generic_only &&
+                     get_adj_kernel(pat, lit, f, plan->precision == kFP32Kahan, g_sq ? sm : 0ull, slices, &jk, &jerr);
     if (!jit && !plan->generic_only) last_jit_error = jerr;
-    const dim3 grid((unsigned)((B + 127) / 128));
+    const dim3 grid((unsigned)(jit ? (B + jk.per_block - 1) / jk.per_block : (B + 127) / 128));
     if (f) {
         PK_FILL_ADJ(float)
         if (jit) {
             void* args[] = {&a};
-            e = cudaLaunchKernel((const void*)jk.fn, grid, dim3(128), args, 0, st);
+            e = cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
         } else {
             e = pk::launch_gen_adj(a, st);
         }
@@ -454,7 +457,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
         PK_FILL_ADJ(double)
         if (jit) {
             void* args[] = {&a};
-            e = cudaLaunchKernel((const void*)jk.fn, grid, dim3(128), args, 0, st);
+            e = cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
         } else {
             e = pk::launch_gen_adj(a, st);
         }

@@ -61,6 +61,7 @@ struct Plan {
     int precision = kFP64;
     bool generic_only = false;
     bool no_literals = false;   // every value loaded: one kernel for all batches
+    int slicing = 0;            // warp-sliced kernels: 0 by size, 1 always, -1 never
     DevBuf gpat;           // flat pattern for the generic kernels (uploaded on first use)
     pk::GenPattern gen() const;
     int ensure_device(std::string* err);

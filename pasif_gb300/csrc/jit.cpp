@@ -11,6 +11,7 @@
 
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <map>
@@ -159,9 +160,400 @@ bool compile(const std::string& src, const char* name, cudaKernel_t* fn, std::st
     return true;
 }
 
+
+// ---- warp-sliced kernels ------------------------------------------------------
+
+struct Term {
+    int q;        // value index
+    int kind;     // 0 K, 1 Gamma, 2 Lambda, 3 Psi, 4 forcing
+    int ops[4];   // state operands in product order (kind + 1 of them; none for forcing)
+};
+
+// Terms of every destination in the canonical order: K row, Gamma, Lambda,
+// Psi, forcing (the order Emitter::rhs and Pattern::flat use).
+std::vector<std::vector<Term>> dest_terms(const Pattern& pat) {
+    const int go = pat.k_nnz(), lo = go + pat.g_nnz(), po = lo + pat.l_nnz(), fo = po + pat.p_nnz();
+    std::vector<std::vector<Term>> t(pat.n);
+    for (int i = 0; i < pat.n; ++i)
+        for (int q = pat.k_ptr[i]; q < pat.k_ptr[i + 1]; ++q) t[i].push_back({q, 0, {pat.k_col[q], 0, 0, 0}});
+    for (int e = 0; e < pat.g_nnz(); ++e) {
+        const int* ix = &pat.g_idx[3 * e];
+        t[ix[0]].push_back({go + e, 1, {ix[1], ix[2], 0, 0}});
+    }
+    for (int e = 0; e < pat.l_nnz(); ++e) {
+        const int* ix = &pat.l_idx[4 * e];
+        t[ix[0]].push_back({lo + e, 2, {ix[1], ix[2], ix[3], 0}});
+    }
+    for (int e = 0; e < pat.p_nnz(); ++e) {
+        const int* ix = &pat.p_idx[5 * e];
+        t[ix[0]].push_back({po + e, 3, {ix[1], ix[2], ix[3], ix[4]}});
+    }
+    for (int e = 0; e < pat.f_nnz(); ++e) t[pat.f_idx[e]].push_back({fo + e, 4, {0, 0, 0, 0}});
+    return t;
+}
+
+struct Slicing {
+    int L = 0;
+    std::vector<int> owner, local, pub;      // per component (pub: -1 = not published)
+    std::vector<std::vector<int>> own;       // per slice: components in local order
+    int NP = 0;
+    int sq_owner = 0;
+};
+
+// Components ordered by reverse Cuthill-McKee on the interaction graph, cut
+// into L contiguous runs of about equal work, so that strongly coupled
+// components share a warp and few values cross warps.
+Slicing make_slicing(const Pattern& pat, const std::vector<std::vector<Term>>& dt, int L, unsigned long long sq_mask,
+                     bool adjoint) {
+    const int n = pat.n;
+    std::vector<std::vector<int>> adj(n);
+    std::vector<double> wt(n, 4.0);
+    for (int i = 0; i < n; ++i)
+        for (const Term& t : dt[i]) {
+            wt[i] += 2.0 + (t.kind < 4 ? t.kind : 0);
+            for (int k = 0; k < (t.kind < 4 ? t.kind + 1 : 0); ++k) {
+                const int j = t.ops[k];
+                if (j != i) { adj[i].push_back(j); adj[j].push_back(i); }
+            }
+        }
+    for (auto& a : adj) {
+        std::sort(a.begin(), a.end());
+        a.erase(std::unique(a.begin(), a.end()), a.end());
+    }
+    std::vector<int> order, seen(n, 0);
+    while ((int)order.size() < n) {
+        int start = -1;
+        for (int i = 0; i < n; ++i)
+            if (!seen[i] && (start < 0 || adj[i].size() < adj[start].size())) start = i;
+        seen[start] = 1;
+        size_t head = order.size();
+        order.push_back(start);
+        while (head < order.size()) {
+            const int v = order[head++];
+            std::vector<int> nb;
+            for (int u : adj[v])
+                if (!seen[u]) { seen[u] = 1; nb.push_back(u); }
+            std::stable_sort(nb.begin(), nb.end(), [&](int x, int y) { return adj[x].size() < adj[y].size(); });
+            order.insert(order.end(), nb.begin(), nb.end());
+        }
+    }
+    std::reverse(order.begin(), order.end());
+    double total = 0.0;
+    for (double w : wt) total += w;
+    Slicing s;
+    s.owner.assign(n, 0);
+    std::vector<std::vector<int>> runs(L);
+    double cum = 0.0;
+    for (int v : order) {
+        int k = (int)((cum + 0.5 * wt[v]) * L / total);
+        k = std::max(0, std::min(L - 1, k));
+        runs[k].push_back(v);
+        cum += wt[v];
+    }
+    for (auto& r : runs)
+        if (!r.empty()) s.own.push_back(r);
+    s.L = (int)s.own.size();
+    s.local.assign(n, 0);
+    for (int w = 0; w < s.L; ++w)
+        for (int k = 0; k < (int)s.own[w].size(); ++k) {
+            s.owner[s.own[w][k]] = w;
+            s.local[s.own[w][k]] = k;
+        }
+    // the lightest slice sums the squares (it reads the others' components)
+    double best = 1e300;
+    for (int w = 0; w < s.L; ++w) {
+        double sw = 0.0;
+        for (int v : s.own[w]) sw += wt[v];
+        if (sw < best) { best = sw; s.sq_owner = w; }
+    }
+    std::vector<char> need(n, 0);
+    for (int i = 0; i < n; ++i)
+        for (const Term& t : dt[i]) {
+            const int no = t.kind < 4 ? t.kind + 1 : 0;
+            for (int k = 0; k < no; ++k)
+                if (s.owner[t.ops[k]] != s.owner[i]) need[t.ops[k]] = 1;
+            if (adjoint) {   // the VJP owner of an operand reads the term's weight and its other operands
+                for (int k = 0; k < no; ++k) {
+                    const int ok = s.owner[t.ops[k]];
+                    if (ok != s.owner[i]) need[i] = 1;
+                    for (int z = 0; z < no; ++z)
+                        if (s.owner[t.ops[z]] != ok) need[t.ops[z]] = 1;
+                }
+            }
+        }
+    for (int i = 0; i < n && i < 64; ++i)
+        if (((sq_mask >> i) & 1ull) && s.owner[i] != s.sq_owner) need[i] = 1;
+    s.pub.assign(n, -1);
+    for (int i = 0; i < n; ++i)
+        if (need[i]) s.pub[i] = s.NP++;
+    return s;
+}
+
+// Source of the warp-sliced forward (mode 0: pk_fwd over FwdArgs), serving-
+// pool (mode 1: pk_pool over PoolArgs) or exact-adjoint (mode 2: pk_adj over
+// AdjArgs) kernel.
+std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, int mode) {
+    const int n = pat.n;
+    const bool adj = mode == 2;
+    const auto dt = dest_terms(pat);
+    const Slicing sl = make_slicing(pat, dt, key.slices, adj ? 0ull : key.sq_mask, adj);
+    auto S = [](long long v) { return std::to_string(v); };
+    // every term in the global order of the VJP scatter (GenSys::vjp): K rows, Gamma, Lambda, Psi, forcing
+    std::vector<std::pair<int, Term>> scatter;   // (destination, term)
+    if (adj) {
+        for (int kind = 0; kind <= 4; ++kind)
+            for (int i = 0; i < n; ++i)
+                for (const Term& t : dt[i])
+                    if (t.kind == kind) scatter.push_back({i, t});
+        std::stable_sort(scatter.begin(), scatter.end(), [](const std::pair<int, Term>& x, const std::pair<int, Term>& y) {
+            return x.second.kind != y.second.kind ? x.second.kind < y.second.kind
+                                                  : (x.second.kind == 0 ? x.first < y.first : x.second.q < y.second.q);
+        });
+    }
+    std::ostringstream o;
+    o << "// generated by pasif_gb300 jit.cpp: warp-sliced "
+      << (mode == 0 ? "forward" : mode == 1 ? "serving pool" : "exact adjoint") << " RK4, n=" << n
+      << " P=" << pat.P() << " slices=" << sl.L << " published=" << sl.NP << "\n";
+    o << "#include \"rk4_core.cuh\"\nnamespace pk {\n";
+    o << "typedef " << (key.f32 ? "float" : "double") << " R;\n";
+    for (int w = 0; w < sl.L; ++w) {
+        const std::vector<int>& own = sl.own[w];
+        const int MM = (int)own.size();
+        auto mine = [&](int j) { return sl.owner[j] == w; };
+        // values this slice reads: loaded slots (absent = literal)
+        std::map<int, int> slot;
+        auto need_val = [&](int q) {
+            const bool is_lit = q < (int)lit.is_lit.size() && lit.is_lit[q] && std::isfinite(lit.value[q]);
+            if (!is_lit && !slot.count(q)) {
+                const int k = (int)slot.size();
+                slot[q] = k;
+            }
+        };
+        bool forced = false;
+        std::vector<int> foreign, pown;   // pown: values of own destinations' terms (gradients kept here)
+        for (int i : own)
+            for (const Term& t : dt[i]) {
+                need_val(t.q);
+                pown.push_back(t.q);
+                if (t.kind == 4) forced = true;
+                for (int k = 0; k < (t.kind < 4 ? t.kind + 1 : 0); ++k)
+                    if (!mine(t.ops[k])) foreign.push_back(t.ops[k]);
+            }
+        std::vector<int> yforeign, wforeign;   // VJP: other operands and weights of terms that touch own components
+        if (adj)
+            for (const auto& it : scatter) {
+                const Term& t = it.second;
+                const int no = t.kind < 4 ? t.kind + 1 : 0;
+                bool touches = mine(it.first);
+                for (int k = 0; k < no; ++k) touches = touches || mine(t.ops[k]);
+                if (!touches) continue;
+                need_val(t.q);
+                if (!mine(it.first)) wforeign.push_back(it.first);
+                for (int k = 0; k < no; ++k)
+                    if (!mine(t.ops[k])) yforeign.push_back(t.ops[k]);
+            }
+        for (auto* v : {&foreign, &yforeign, &wforeign}) {
+            std::sort(v->begin(), v->end());
+            v->erase(std::unique(v->begin(), v->end()), v->end());
+        }
+        std::sort(pown.begin(), pown.end());
+        std::map<int, int> pslot;
+        for (int q : pown) pslot[q] = (int)pslot.size();
+        auto val = [&](int q) { return slot.count(q) ? "p[" + S(slot[q]) + "]" : hexlit(lit.value[q]); };
+        auto x = [&](int j) { return mine(j) ? "X[" + S(sl.local[j]) + "]" : "x" + S(j); };
+        o << "struct SL" << w << " {\n";
+        o << "  static constexpr int MM = " << MM << ", NP = " << sl.NP << ", PO = " << std::max<size_t>(pown.size(), 1)
+          << ";\n";
+        o << "  static constexpr bool FORCED = " << (forced ? "true" : "false")
+          << ", SQOWN = " << (w == sl.sq_owner ? "true" : "false") << ";\n";
+        o << "  R p[" << std::max<size_t>(slot.size(), 1) << "];\n";
+        o << "  __device__ __forceinline__ void load(const R* __restrict__ vals, long long B, int b) {\n";
+        for (auto& kv : slot) o << "    p[" << kv.second << "] = vals[" << kv.first << "LL * B + b];\n";
+        o << "  }\n";
+        o << "  template <class V> __device__ __forceinline__ void load_vec(V& X, const R* __restrict__ src, long long B,"
+             " int b) const {\n";
+        for (int k = 0; k < MM; ++k) o << "    X[" << k << "] = src[" << own[k] << "LL * B + b];\n";
+        o << "  }\n";
+        o << "  template <class V> __device__ __forceinline__ void store_vec(const V& X, R* dst, long long B, int b)"
+             " const {\n";
+        for (int k = 0; k < MM; ++k) o << "    dst[" << own[k] << "LL * B + b] = X[" << k << "];\n";
+        o << "  }\n";
+        o << "  template <class V> __device__ __forceinline__ void store_traj(const V& X, R* dst, long long B, int b)"
+             " const { store_vec(X, dst, B, b); }\n";
+        o << "  template <class V> __device__ __forceinline__ void publish(const V& X, R* buf) const {\n";
+        for (int k = 0; k < MM; ++k)
+            if (sl.pub[own[k]] >= 0) o << "    buf[" << sl.pub[own[k]] * 32 << "] = X[" << k << "];\n";
+        o << "  }\n";
+        o << "  template <class V> __device__ __forceinline__ void track_max(const V& X, V& Mx) const {\n";
+        for (int k = 0; k < MM; ++k)
+            if (own[k] < 64 && ((key.max_mask >> own[k]) & 1ull))
+                o << "    Mx[" << k << "] = M<R>::max(Mx[" << k << "], M<R>::abs(X[" << k << "]));\n";
+        o << "  }\n";
+        o << "  template <class V> __device__ __forceinline__ void store_max(const V& Mx, R* out, long long B, int b)"
+             " const {\n";
+        {
+            int rank = 0;
+            for (int i = 0; i < n && i < 64; ++i)
+                if ((key.max_mask >> i) & 1ull) {
+                    if (sl.owner[i] == w) o << "    out[" << rank << "LL * B + b] = Mx[" << sl.local[i] << "];\n";
+                    ++rank;
+                }
+        }
+        o << "  }\n";
+        o << "  template <bool KAHAN, class V> __device__ __forceinline__ void add_sq(const V& X, const R* buf, R& sq,"
+             " R& sqc) const {\n";
+        if (w == sl.sq_owner) {
+            o << "    typedef M<R> m;\n";
+            for (int i = 0; i < n && i < 64; ++i)
+                if ((key.sq_mask >> i) & 1ull) {
+                    const std::string q = sl.owner[i] == w ? "X[" + S(sl.local[i]) + "]" : "buf[" + S(sl.pub[i] * 32) + "]";
+                    o << "    { const R q = " << q << ";\n";
+                    o << "      if (KAHAN) { const R y = m::sub(m::mul(q, q), sqc); const R t = m::add(sq, y);"
+                         " sqc = m::sub(m::sub(t, sq), y); sq = t; } else { sq = m::fma(q, q, sq); } }\n";
+                }
+        }
+        o << "  }\n";
+        o << "  template <class V, class F> __device__ __forceinline__ void rhs(const V& X, const R* buf, R u, F& f)"
+             " const {\n";
+        o << "    typedef M<R> m;\n    R a, c;\n";
+        for (int j : foreign) o << "    const R x" << j << " = buf[" << sl.pub[j] * 32 << "];\n";
+        for (int k = 0; k < MM; ++k) {
+            const int i = own[k];
+            const std::vector<Term>& ts = dt[i];
+            if (ts.empty()) {
+                o << "    f[" << k << "] = R(0);\n";
+                continue;
+            }
+            for (size_t e = 0; e < ts.size(); ++e) {
+                const Term& t = ts[e];
+                std::string first, last;
+                if (t.kind == 4) {
+                    first = val(t.q);
+                    last = "u";
+                } else {
+                    first = val(t.q);
+                    for (int z = 0; z < t.kind; ++z) first = "m::mul(" + first + ", " + x(t.ops[z]) + ")";
+                    last = x(t.ops[t.kind]);
+                }
+                const char* acc = (e & 1) ? "c" : "a";
+                if (e < 2) o << "    " << acc << " = m::mul(" << first << ", " << last << ");\n";
+                else o << "    " << acc << " = m::fma(" << first << ", " << last << ", " << acc << ");\n";
+            }
+            o << "    f[" << k << "] = " << (ts.size() >= 2 ? "m::add(a, c)" : "a") << ";\n";
+        }
+        o << "  }\n";
+        if (adj) {
+            auto W = [&](int i) { return mine(i) ? "W[" + S(sl.local[i]) + "]" : "w" + S(i); };
+            auto Y = [&](int j) { return mine(j) ? "Y[" + S(sl.local[j]) + "]" : "y" + S(j); };
+            auto out = [&](int j) { return "out[" + S(sl.local[j]) + "]"; };
+            o << "  template <class V, class PA> __device__ __forceinline__ void vjp(const V& Y, const R* yb, const V& W,"
+                 " const R* wb, R u, V& out, PA& pacc) const {\n";
+            o << "    typedef M<R> m;\n";
+            for (int j : yforeign) o << "    const R y" << j << " = yb[" << sl.pub[j] * 32 << "];\n";
+            for (int i : wforeign) o << "    const R w" << i << " = wb[" << sl.pub[i] * 32 << "];\n";
+            for (int k = 0; k < MM; ++k) o << "    out[" << k << "] = R(0);\n";
+            for (const auto& it : scatter) {
+                const int i = it.first;
+                const Term& t = it.second;
+                const int no = t.kind < 4 ? t.kind + 1 : 0;
+                bool any = false;
+                for (int k = 0; k < no; ++k) any = any || mine(t.ops[k]);
+                const std::string ps = mine(i) ? "pacc[" + S(pslot[t.q]) + "]" : "";
+                if (t.kind == 0) {
+                    const int j = t.ops[0];
+                    if (mine(j)) o << "    " << out(j) << " = m::fma(" << val(t.q) << ", " << W(i) << ", " << out(j) << ");\n";
+                    if (mine(i)) o << "    pacc_add(" << ps << ", " << W(i) << ", " << Y(j) << ");\n";
+                } else if (t.kind == 4) {
+                    if (mine(i)) o << "    pacc_add(" << ps << ", " << W(i) << ", u);\n";
+                } else {
+                    if (any) {
+                        o << "    { const R a_ = m::mul(" << val(t.q) << ", " << W(i) << ");\n";
+                        for (int k = 0; k < no; ++k) {
+                            const int j = t.ops[k];
+                            if (!mine(j)) continue;
+                            // product of the other operands in operand order; the last one is the fma factor
+                            std::vector<int> oth;
+                            for (int z = 0; z < no; ++z)
+                                if (z != k) oth.push_back(t.ops[z]);
+                            std::string f = "a_";
+                            for (size_t z = 0; z + 1 < oth.size(); ++z) f = "m::mul(" + f + ", " + Y(oth[z]) + ")";
+                            o << "      " << out(j) << " = m::fma(" << f << ", " << Y(oth.back()) << ", " << out(j)
+                              << ");\n";
+                        }
+                        o << "    }\n";
+                    }
+                    if (mine(i)) {
+                        std::string f = W(i);
+                        for (int z = 0; z + 1 < no; ++z) f = "m::mul(" + f + ", " + Y(t.ops[z]) + ")";
+                        o << "    pacc_add(" << ps << ", " << f << ", " << Y(t.ops[no - 1]) << ");\n";
+                    }
+                }
+            }
+            o << "  }\n";
+            o << "  template <class V> __device__ __forceinline__ void add_sq_grad(V& LAM, const V& QN, R g) const {\n";
+            for (int k = 0; k < MM; ++k)
+                if (own[k] < 64 && ((key.sq_mask >> own[k]) & 1ull))
+                    o << "    LAM[" << k << "] = M<R>::fma(g, QN[" << k << "], LAM[" << k << "]);\n";
+            o << "  }\n";
+            o << "  template <class PV> __device__ __forceinline__ void store_pbar(const PV& PB, double* pbar, long long B,"
+                 " int b) const {\n";
+            for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = PB[" << kv.second << "];\n";
+            o << "  }\n";
+            o << "  __device__ __forceinline__ void zero_pbar(double* pbar, long long B, int b) const {\n";
+            for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = 0.0;\n";
+            o << "  }\n";
+            o << "  template <class PV> __device__ __forceinline__ void add_pbar(const PV& ps, double* pbar, long long B,"
+                 " int b) const {\n";
+            for (auto& kv : pslot)
+                o << "    pbar[" << kv.first << "LL * B + b] = pbar[" << kv.first << "LL * B + b] + (double)ps["
+                  << kv.second << "];\n";
+            o << "  }\n";
+        }
+        o << "};\n";
+    }
+    o << "}  // namespace pk\n";
+    const std::string kahan = key.kahan ? "true" : "false", hmax = key.max_mask ? "true" : "false",
+                      hsq = key.sq_mask ? "true" : "false", htraj = key.traj ? "true" : "false";
+    const char* sig = mode == 0 ? "pk_fwd(pk::FwdArgs<pk::R> a)" : mode == 1 ? "pk_pool(pk::PoolArgs<pk::R> p)"
+                                                                            : "pk_adj(pk::AdjArgs<pk::R> a)";
+    o << "extern \"C\" __global__ void __launch_bounds__(" << 32 * sl.L << ") " << sig << " {\n";
+    o << "  using namespace pk;\n";
+    o << "  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;\n";
+    o << "  const long long bb = (long long)blockIdx.x * 32 + lane;\n";
+    o << "  const long long cnt = " << (mode == 1 ? "p.C" : "a.B") << ";\n";
+    o << "  const bool valid = bb < cnt;\n";
+    o << "  const int b = valid ? (int)bb : (int)cnt - 1;\n";
+    o << "  R* sm = reinterpret_cast<R*>(pk_dyn_smem()) + lane;\n";
+    o << "  switch (w) {\n";
+    for (int w = 0; w < sl.L; ++w) {
+        o << "    case " << w << ": { SL" << w << " sl; ";
+        if (mode == 1)
+            o << "ws_pool<R, " << kahan << ", " << hmax << ", " << hsq << ", " << n << ">(sl, p, sm, b, valid, w);";
+        else if (mode == 0)
+            o << "ws_fwd<R, " << kahan << ", " << hmax << ", " << hsq << ", " << htraj << ", " << n
+              << ">(sl, a, sm, b, valid);";
+        else   // the Kahan mode of the forward passes is the plan's (AdjArgs::kahan)
+            o << "ws_adj<R, " << kahan << ", " << hsq << ", " << (key.f32 ? "true" : "false") << ", " << n
+              << ">(sl, a, sm, b, valid);";
+        o << " } break;\n";
+    }
+    o << "    default: break;\n  }\n}\n";
+    o << "// ws-launch " << 32 * sl.L << " " << (adj ? 6 : 2) * sl.NP * 32 * (key.f32 ? 4 : 8) << "\n";
+    return o.str();
+}
+
+// Launch shape recorded by ws_source on its last line.
+void ws_launch(const std::string& src, int* block, int* smem) {
+    const size_t at = src.rfind("// ws-launch ");
+    *block = 128;
+    *smem = 0;
+    if (at != std::string::npos) std::sscanf(src.c_str() + at, "// ws-launch %d %d", block, smem);
+}
+
 }  // namespace
 
 std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key) {
+    if (key.slices >= 2) return ws_source(pat, lit, key, 0);
     Emitter em(pat, lit);
     const int n = pat.n;
     std::ostringstream o;
@@ -303,7 +695,19 @@ bool get_cached(const std::string& src, const char* name, int block, JitKernel* 
     }
     JitKernel k;
     k.block = block;
+    k.per_block = block;
+    if (src.find("// ws-launch ") != std::string::npos) {
+        ws_launch(src, &k.block, &k.smem);
+        k.per_block = 32;
+    }
     if (!compile(src, name, &k.fn, err)) return false;
+    if (k.smem > 48 * 1024) {
+        cudaError_t ce = cudaFuncSetAttribute((const void*)k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem);
+        if (ce != cudaSuccess) {
+            *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ce);
+            return false;
+        }
+    }
     cudaFuncAttributes attr;
     if (cudaFuncGetAttributes(&attr, (const void*)k.fn) == cudaSuccess) {
         k.regs = attr.numRegs;
@@ -321,7 +725,16 @@ bool compile_report(const std::string& src, std::string* report, std::string* er
     return to_cubin(src, &cubin, report, err);
 }
 
-std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask) {
+std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, int slices,
+                       bool kahan) {
+    if (slices >= 2) {
+        FwdKernelKey key;
+        key.f32 = f32;
+        key.kahan = kahan;
+        key.sq_mask = sq_mask;
+        key.slices = slices;
+        return ws_source(pat, lit, key, 2);
+    }
     Emitter em(pat, lit);
     std::ostringstream o;
     o << "// generated by pasif_gb300 jit.cpp: exact adjoint, n=" << pat.n << " P=" << pat.P() << "\n";
@@ -348,6 +761,7 @@ std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsign
 }
 
 std::string pool_source(const Pattern& pat, const FwdKernelKey& key) {
+    if (key.slices >= 2) return ws_source(pat, Literals(), key, 1);
     Literals none;   // a pool's slots change owner: every value is loaded
     Emitter em(pat, none);
     std::ostringstream o;
@@ -377,47 +791,38 @@ std::string pool_source(const Pattern& pat, const FwdKernelKey& key) {
 }
 
 bool get_pool_kernel(const Pattern& pat, const FwdKernelKey& key, JitKernel* out, std::string* err) {
-    if (pat.n <= 0 || pat.n > kJitMaxN) {
+    if (pat.n <= 0 || pat.n > (key.slices >= 2 ? kWsMaxN : kJitMaxN)) {
         *err = "state size outside the specialised range";
         return false;
     }
     return get_cached(pool_source(pat, key), "pk_pool", key.block, out, err);
 }
 
-bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, JitKernel* out,
-                    std::string* err) {
-    if (pat.n <= 0 || pat.n > kJitMaxN || pat.P() > 1024) {
+bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, bool kahan, unsigned long long sq_mask, int slices,
+                    JitKernel* out, std::string* err) {
+    if (pat.n <= 0 || pat.n > (slices >= 2 ? kWsMaxN : kJitMaxN) || pat.P() > (slices >= 2 ? 8192 : 1024)) {
         *err = "pattern outside the specialised range";
         return false;
     }
-    return get_cached(adj_source(pat, lit, f32, sq_mask), "pk_adj", 128, out, err);
+    return get_cached(adj_source(pat, lit, f32, sq_mask, slices, kahan), "pk_adj", 128, out, err);
 }
 
 bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, JitKernel* out,
                     std::string* err) {
-    if (pat.n <= 0 || pat.n > kJitMaxN) {
+    if (pat.n <= 0 || pat.n > (key.slices >= 2 ? kWsMaxN : kJitMaxN)) {
         *err = "state size outside the specialised range";
         return false;
     }
-    const std::string src = fwd_source(pat, lit, key);
-    Cache& c = cache();
-    std::lock_guard<std::mutex> lk(c.mu);
-    auto it = c.fwd.find(src);
-    if (it != c.fwd.end()) {
-        *out = it->second;
-        return true;
-    }
-    JitKernel k;
-    k.block = key.block;
-    if (!compile(src, "pk_fwd", &k.fn, err)) return false;
-    cudaFuncAttributes attr;
-    if (cudaFuncGetAttributes(&attr, (const void*)k.fn) == cudaSuccess) {
-        k.regs = attr.numRegs;
-        k.local_bytes = (int)attr.localSizeBytes;
-    }
-    c.fwd[src] = k;
-    *out = k;
-    return true;
+    return get_cached(fwd_source(pat, lit, key), "pk_fwd", key.block, out, err);
+}
+
+int ws_slices(const Pattern& pat, bool f32, bool force) {
+    const int n = pat.n;
+    // measured crossover on GB300: thread per system wins below ~28 states in FP32, ~24 in FP64
+    if (n < 2 || n > kWsMaxN || (!force && n < (f32 ? 28 : 24))) return 0;
+    const int cpw = force ? 2 : (f32 ? 8 : 6);   // components per warp
+    const int L = (n + cpw - 1) / cpw;
+    return std::max(2, std::min(16, std::min(L, n)));
 }
 
 }  // namespace pasif

@@ -26,14 +26,22 @@ struct FwdKernelKey {
     int block = 128;
     int window = 0;                 // forcing window (0 = sample and hold)
     std::vector<double> wn, wc;     // its weights in the compute precision
+    int slices = 0;                 // >= 2: warp-sliced kernel with that many warps per 32 systems
 };
 
 struct JitKernel {
     cudaKernel_t fn = nullptr;
-    int block = 128;
+    int block = 128;                // threads per block
+    int per_block = 128;            // systems per block (32 for warp-sliced kernels)
+    int smem = 0;                   // dynamic shared memory bytes
     int regs = 0;
     int local_bytes = 0;
 };
+
+// Warps per 32 systems of the warp-sliced kernels for a pattern: 0 (thread
+// per system) below the size where the register-resident vectors spill,
+// unless `force`.
+int ws_slices(const Pattern& pat, bool f32, bool force);
 
 // Source of the forward kernel for a pattern (exposed for tests and docs).
 std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key);
@@ -44,8 +52,11 @@ bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey&
                     JitKernel* out, std::string* err);
 
 // Source and cached kernel of the exact adjoint (AdjArgs) for a pattern.
-std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask);
-bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, JitKernel* out,
+// (slices >= 2: warp-sliced, with the forward passes' Kahan mode compiled in)
+std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, int slices = 0,
+                       bool kahan = false);
+bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, bool kahan, unsigned long long sq_mask, int slices,
+                    JitKernel* out,
                     std::string* err);
 // Serving-pool chunk kernel (PoolArgs): values always loaded, no literals.
 std::string pool_source(const Pattern& pat, const FwdKernelKey& key);
@@ -58,7 +69,9 @@ bool compile_report(const std::string& src, std::string* report, std::string* er
 bool fwd_compile_report(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, std::string* report,
                         std::string* err);
 
-// Largest state size the register-resident specialisation accepts.
+// Largest state size the register-resident specialisation accepts (thread
+// per system, and warp-sliced).
 constexpr int kJitMaxN = 128;
+constexpr int kWsMaxN = 256;
 
 }  // namespace pasif

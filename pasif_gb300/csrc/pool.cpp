@@ -42,7 +42,7 @@ Pool::~Pool() {
 
 int Pool::create(const Pattern& pat, int precision, int window, const double* im, double h,
                  const std::vector<int>& max_comp, const std::vector<int>& sq_comp, int capacity,
-                 long long arena_samples, int chunk, std::unique_ptr<Pool>* out, std::string* err) {
+                 long long arena_samples, int chunk, int slicing, std::unique_ptr<Pool>* out, std::string* err) {
     if (capacity < 1 || arena_samples < 1 || chunk < 1) { *err = "pool sizes must be positive"; return 1; }
     if (window < 0 || (window > 0 && ((window & (window - 1)) || !im))) {
         *err = "window must be 0 or a power of two with weights";
@@ -112,6 +112,7 @@ int Pool::create(const Pattern& pat, int precision, int window, const double* im
     key.max_mask = p->max_mask_;
     key.sq_mask = p->sq_mask_;
     key.window = window;
+    key.slices = slicing < 0 ? 0 : ws_slices(pat, f32, slicing > 0);
     for (int i = 0; i < 2 * window; ++i) {
         const double w = f32 ? (double)(float)im[i] : im[i];
         p->im_.push_back(im[i]);
@@ -157,7 +158,7 @@ int Pool::build_graph(std::string* err) {
         a.C = C_;
         a.chunk = chunk_;
     };
-    const dim3 grid((unsigned)((C_ + k_.block - 1) / k_.block));
+    const dim3 grid((unsigned)((C_ + k_.per_block - 1) / k_.per_block));
     cudaGraph_t g = nullptr;
     PL_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     cudaError_t e;
@@ -165,12 +166,12 @@ int Pool::build_graph(std::string* err) {
         pk::PoolArgs<float> a;
         fill(a, 0.0f);
         void* args[] = {&a};
-        e = cudaLaunchKernel((const void*)k_.fn, grid, dim3(k_.block), args, 0, st_);
+        e = cudaLaunchKernel((const void*)k_.fn, grid, dim3(k_.block), args, (size_t)k_.smem, st_);
     } else {
         pk::PoolArgs<double> a;
         fill(a, 0.0);
         void* args[] = {&a};
-        e = cudaLaunchKernel((const void*)k_.fn, grid, dim3(k_.block), args, 0, st_);
+        e = cudaLaunchKernel((const void*)k_.fn, grid, dim3(k_.block), args, (size_t)k_.smem, st_);
     }
     cudaError_t e2 = cudaStreamEndCapture(st_, &g);
     PL_CUDA(e, "pool kernel capture");

@@ -33,7 +33,8 @@ public:
     ~Pool();
     static int create(const Pattern& pat, int precision, int window, const double* im, double h,
                       const std::vector<int>& max_comp, const std::vector<int>& sq_comp, int capacity,
-                      long long arena_samples, int chunk, std::unique_ptr<Pool>* out, std::string* err);
+                      long long arena_samples, int chunk, int slicing, std::unique_ptr<Pool>* out,
+                      std::string* err);
     // PASIF_ERR_STATE (5) when slots or arena space are short: retry later.
     int admit(int n_sys, const double* values, const double* x0, const int* exc_index, const double* signals,
               int n_exc, int len, int nsteps, int max_start, int sq_start, int* req_id, std::string* err);

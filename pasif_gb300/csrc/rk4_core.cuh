@@ -794,4 +794,336 @@ __device__ void refgrad_run_generic(const FSys& fs, const BSys& bs, const RefGra
     for (int i = 0; i < na; ++i) a.out[i * B + b] = A[i];
 }
 
+
+// ---- warp-sliced systems ----------------------------------------------------
+// For large state sizes the L warps of a block share 32 systems (lane = system):
+// warp w owns a slice of the components (its state, compensation, stage vectors
+// and the values of its destinations' terms in registers) and computes the
+// right-hand side of its own destinations in the canonical order.  The
+// components another slice reads are published to shared memory after every
+// stage ([2 buffers][NP published][32 lanes]; a stage reads one buffer and
+// writes the other, so one CTA barrier per stage suffices).  The warps run
+// different (generated) code, so the barrier is the non-aligned
+// barrier.sync, which may be reached from different instructions.  Every
+// component sees the same operations in the same order as in rk4_step, so
+// the results equal the thread-per-system kernels and the oracle bit for bit.
+#ifndef PK_HOST_EMU
+__device__ __forceinline__ unsigned char* pk_dyn_smem() {
+    extern __shared__ __align__(16) unsigned char pk_smem_[];
+    return pk_smem_;
+}
+__device__ __forceinline__ void pk_block_sync() { asm volatile("barrier.sync 0;" ::: "memory"); }
+__device__ __forceinline__ unsigned pk_warp_max(unsigned v) { return __reduce_max_sync(0xffffffffu, v); }
+#endif
+
+// Steps rc.nsteps (<= T) of one system from rc.step0 with the block-uniform
+// trip count T: steps past the system's own count leave its state and
+// reducers untouched (serving pools mix slots at different steps in a block).
+// `out` enables the stores of this lane (trajectory).
+// One RK4 step of the slice (the operations of rk4_step): Q's foreign
+// components are read from b0, the stage vectors pass through b1 and b0, and
+// the new Q is published to b0.  act = false leaves Q and Cm unchanged.
+template <typename R, bool KAHAN, class SL, class V>
+__device__ __forceinline__ void ws_step(const SL& sl, R* b0, R* b1, V& Q, V& Cm, V& S, V& K, V& Mi, R ua, R ub,
+                                        R uc, R h, R h2, R h6, bool act) {
+    typedef M<R> m;
+    constexpr int MM = SL::MM;
+    sl.rhs(Q, b0, ua, K);
+#pragma unroll
+    for (int i = 0; i < MM; ++i) { S[i] = K[i]; Mi[i] = m::fma(h2, K[i], Q[i]); }
+    sl.publish(Mi, b1);
+    pk_block_sync();
+    sl.rhs(Mi, b1, ub, K);
+#pragma unroll
+    for (int i = 0; i < MM; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(h2, K[i], Q[i]); }
+    sl.publish(Mi, b0);
+    pk_block_sync();
+    sl.rhs(Mi, b0, ub, K);
+#pragma unroll
+    for (int i = 0; i < MM; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(h, K[i], Q[i]); }
+    sl.publish(Mi, b1);
+    pk_block_sync();
+    sl.rhs(Mi, b1, uc, K);
+#pragma unroll
+    for (int i = 0; i < MM; ++i) {
+        const R sum = m::add(S[i], K[i]);
+        if (KAHAN) {
+            const R inc = m::mul(h6, sum);
+            const R y = m::sub(inc, Cm[i]);
+            const R t = m::add(Q[i], y);
+            const R c = m::sub(m::sub(t, Q[i]), y);
+            if (act) { Cm[i] = c; Q[i] = t; }
+        } else {
+            const R t = m::fma(h6, sum, Q[i]);
+            if (act) Q[i] = t;
+        }
+    }
+    sl.publish(Q, b0);
+    pk_block_sync();
+}
+
+template <typename R, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, int N, class SL, class V>
+__device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const Forcing<R>& frc, R* sm, int b,
+                                        bool out, const RunCtx& rc, unsigned T, V& Q, V& Cm, V& Mx, R& sq,
+                                        R& sqc) {
+    R* const b0 = sm;
+    R* const b1 = sm + SL::NP * 32;
+    const long long B = a.B;
+    V S, K, Mi;
+    sl.publish(Q, b0);
+    pk_block_sync();
+    R uc = SL::FORCED ? force_at(frc, rc.ebase, rc.step0, 0u, 0u) : R(0);
+    for (unsigned s = 0; s < T; ++s) {
+        const bool act = s < rc.nsteps;
+        const unsigned step = rc.step0 + s;
+        const R ua = uc;
+        R ub = R(0);
+        if (SL::FORCED) {
+            ub = force_at(frc, rc.ebase, step, 0u, 1u);
+            uc = force_at(frc, rc.ebase, step, 1u, 0u);
+        }
+        ws_step<R, KAHAN>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act);
+        if (act) {
+            if (HTRAJ && out && step % (unsigned)a.traj_every == 0u) {
+                const long long slot = (long long)(step / (unsigned)a.traj_every) -
+                                       (long long)(a.step0 / (unsigned)a.traj_every) -
+                                       ((a.step0 % (unsigned)a.traj_every) ? 1 : 0);
+                if (slot >= 0 && slot < a.traj_slots) sl.store_traj(Q, a.traj + slot * N * B, B, b);
+            }
+            if (HMAX && (long long)step >= (long long)rc.max_start) sl.track_max(Q, Mx);
+            if (HSQ && SL::SQOWN && (long long)step >= (long long)rc.sq_start) sl.template add_sq<KAHAN>(Q, b0, sq, sqc);
+        }
+    }
+}
+
+// Batch forward (FwdArgs): lane b of every warp of the block; `valid` is false
+// for the lanes past the batch, which run a copy of the last system and store
+// nothing.
+template <typename R, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, int N, class SL>
+__device__ __forceinline__ void ws_fwd(SL& sl, const FwdArgs<R>& a, R* sm, int b, bool valid) {
+    typedef RegVec<R, SL::MM> V;
+    const long long B = a.B;
+    sl.load(a.vals, B, b);
+    V Q, Cm, Mx;
+    sl.load_vec(Q, a.state, B, b);
+#pragma unroll
+    for (int i = 0; i < SL::MM; ++i) { Cm[i] = R(0); Mx[i] = R(0); }
+    R sq = R(0), sqc = R(0);
+    RunCtx rc;
+    rc.ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+    rc.step0 = a.step0;
+    rc.nsteps = (unsigned)a.nsteps;
+    rc.max_start = a.max_start;
+    rc.sq_start = a.sq_start;
+    ws_core<R, KAHAN, HMAX, HSQ, HTRAJ, N>(sl, a, a.frc, sm, b, valid, rc, (unsigned)a.nsteps, Q, Cm, Mx, sq, sqc);
+    if (!valid) return;
+    sl.store_vec(Q, a.state, B, b);
+    if (HMAX) sl.store_max(Mx, a.out_max, B, b);
+    if (HSQ && SL::SQOWN) a.out_sq[b] = sq;
+}
+
+// Serving-pool chunk (PoolArgs), as pool_run_iv: every busy slot of the
+// block's 32 advances min(chunk, remaining) steps; warp 0 books the steps.
+template <typename R, bool KAHAN, bool HMAX, bool HSQ, int N, class SL>
+__device__ __forceinline__ void ws_pool(SL& sl, const PoolArgs<R>& p, R* sm, int b, bool valid, int warp) {
+    typedef RegVec<R, SL::MM> V;
+    const int rem = valid ? p.remain[b] : 0;
+    const unsigned mine = rem > 0 ? (unsigned)(rem < p.chunk ? rem : p.chunk) : 0u;
+    const unsigned T = pk_warp_max(mine);   // every warp of the block holds the same 32 slots
+    if (T == 0u) return;
+    const long long C = p.C;
+    sl.load(p.vals, C, b);
+    V Q, Cm, Mx;
+    sl.load_vec(Q, p.state, C, b);
+    if (KAHAN) sl.load_vec(Cm, p.comp, C, b);
+    else {
+#pragma unroll
+        for (int i = 0; i < SL::MM; ++i) Cm[i] = R(0);
+    }
+    if (HMAX) sl.load_vec(Mx, p.mx, C, b);
+    else {
+#pragma unroll
+        for (int i = 0; i < SL::MM; ++i) Mx[i] = R(0);
+    }
+    R sq = (HSQ && SL::SQOWN) ? p.sq[b] : R(0), sqc = (HSQ && SL::SQOWN) ? p.sqc[b] : R(0);
+    FwdArgs<R> a;
+    a.B = p.C;
+    a.h = p.h;
+    a.h2 = p.h2;
+    a.h6 = p.h6;
+    a.traj = nullptr;
+    a.traj_every = 1;
+    a.traj_slots = 0;
+    a.step0 = 0;
+    Forcing<R> frc = p.frc;
+    frc.len = p.len[b];
+    frc.total = p.lim[b];
+    RunCtx rc;
+    rc.ebase = p.ebase[b];
+    rc.step0 = p.step[b];
+    rc.nsteps = mine;
+    rc.max_start = p.max_start[b];
+    rc.sq_start = p.sq_start[b];
+    ws_core<R, KAHAN, HMAX, HSQ, false, N>(sl, a, frc, sm, b, false, rc, T, Q, Cm, Mx, sq, sqc);
+    if (mine == 0u) return;
+    sl.store_vec(Q, p.state, C, b);
+    if (KAHAN) sl.store_vec(Cm, p.comp, C, b);
+    if (HMAX) sl.store_vec(Mx, p.mx, C, b);
+    if (HSQ && SL::SQOWN) { p.sq[b] = sq; p.sqc[b] = sqc; }
+    if (warp == 0) {
+        p.step[b] = rc.step0 + mine;
+        p.remain[b] = rem - (int)mine;
+    }
+}
+
+// Exact discrete adjoint, warp-sliced (the algorithm and operation order of
+// adj_run_jit).  Shared memory: regions for QC, Y2, Y3, Y4 (the first two
+// double as the forward passes' stage buffers) and two for the VJP weights
+// KB, each [NP][32].  The VJP of a slice is its gather form: the owner of
+// component j adds every contribution to out[j] in the global scatter order
+// of GenSys::vjp; the owner of destination i accumulates the gradients of the
+// values of i's terms (PO of them: FP64 totals, STEP_ACC: per-step FP32 sums
+// first).
+template <typename R, bool KAHAN, bool HSQ, bool STEP_ACC, int N, class SL>
+__device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b, bool valid) {
+    typedef M<R> m;
+    typedef RegVec<R, SL::MM> V;
+    constexpr int MM = SL::MM, NP = SL::NP, PO = SL::PO;
+    const long long B = a.B;
+    R* const rq = sm;
+    R* const r2 = sm + NP * 32;
+    R* const r3 = sm + 2 * NP * 32;
+    R* const r4 = sm + 3 * NP * 32;
+    R* const k0 = sm + 4 * NP * 32;
+    R* const k1 = sm + 5 * NP * 32;
+    sl.load(a.vals, B, b);
+    const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+    // FP64 totals: in registers (FP64 path), or in pbar itself when the FP32
+    // per-step sums (pst) are added once per step (keeps registers for the vectors)
+    RegVec<double, STEP_ACC ? 1 : PO> PB;
+    RegVec<R, STEP_ACC ? PO : 1> pst;
+#pragma unroll
+    for (int p = 0; p < (STEP_ACC ? 1 : PO); ++p) PB[p] = 0.0;
+#pragma unroll
+    for (int p = 0; p < (STEP_ACC ? PO : 1); ++p) pst[p] = R(0);
+    if constexpr (STEP_ACC) {
+        if (valid) sl.zero_pbar(a.pbar, B, b);
+    }
+    V Q, Cm, S, K, Mi;
+    sl.load_vec(Q, a.x0, B, b);
+#pragma unroll
+    for (int i = 0; i < MM; ++i) Cm[i] = R(0);
+    sl.publish(Q, rq);
+    pk_block_sync();
+    for (int t = 0; t < a.nsteps; ++t) {
+        if (t % a.C == 0 && valid) {
+            R* ck = a.ckpt + (long long)(t / a.C) * 2 * N * B;
+            sl.store_vec(Q, ck, B, b);
+            sl.store_vec(Cm, ck + (long long)N * B, B, b);
+        }
+        const unsigned st = (unsigned)t;
+        const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+        const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+        const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+        ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
+    }
+    V LAM, QN;
+    if (a.g_final) sl.load_vec(LAM, a.g_final, B, b);
+    else {
+#pragma unroll
+        for (int i = 0; i < MM; ++i) LAM[i] = R(0);
+    }
+    const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
+    for (int k = a.nck - 1; k >= 0; --k) {
+        const int start = k * a.C;
+        const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
+        const R* ck = a.ckpt + (long long)k * 2 * N * B;
+        sl.load_vec(Q, ck, B, b);
+        sl.load_vec(Cm, ck + (long long)N * B, B, b);
+        sl.publish(Q, rq);
+        pk_block_sync();
+        for (int t = start; t < end; ++t) {
+            if (valid) sl.store_vec(Q, a.buf + (long long)(t - start) * N * B, B, b);
+            const unsigned st = (unsigned)t;
+            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
+        }
+#pragma unroll
+        for (int i = 0; i < MM; ++i) QN[i] = Q[i];
+        for (int t = end - 1; t >= start; --t) {
+            V QC, Y2, Y3, Y4, QB, KB, YB;
+            // the chunk states were written by this thread (own components) before the barriers above
+            sl.load_vec(QC, a.buf + (long long)(t - start) * N * B, B, b);
+            if (HSQ && a.g_sq && t >= a.sq_start) sl.add_sq_grad(LAM, QN, gsq2h);
+            const unsigned st = (unsigned)t;
+            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            sl.publish(QC, rq);
+            pk_block_sync();
+            sl.rhs(QC, rq, ua, K);
+#pragma unroll
+            for (int i = 0; i < MM; ++i) Y2[i] = m::fma(a.h2, K[i], QC[i]);
+            sl.publish(Y2, r2);
+            pk_block_sync();
+            sl.rhs(Y2, r2, ub, K);
+#pragma unroll
+            for (int i = 0; i < MM; ++i) Y3[i] = m::fma(a.h2, K[i], QC[i]);
+            sl.publish(Y3, r3);
+            pk_block_sync();
+            sl.rhs(Y3, r3, ub, K);
+#pragma unroll
+            for (int i = 0; i < MM; ++i) { Y4[i] = m::fma(a.h, K[i], QC[i]); KB[i] = m::mul(a.h6, LAM[i]); QB[i] = LAM[i]; }
+            sl.publish(Y4, r4);
+            sl.publish(KB, k0);
+            pk_block_sync();
+            if constexpr (STEP_ACC) sl.vjp(Y4, r4, KB, k0, uc, YB, pst);
+            else sl.vjp(Y4, r4, KB, k0, uc, YB, PB);
+#pragma unroll
+            for (int i = 0; i < MM; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h, YB[i], m::mul(R(2), sb));
+            }
+            sl.publish(KB, k1);
+            pk_block_sync();
+            if constexpr (STEP_ACC) sl.vjp(Y3, r3, KB, k1, ub, YB, pst);
+            else sl.vjp(Y3, r3, KB, k1, ub, YB, PB);
+#pragma unroll
+            for (int i = 0; i < MM; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h2, YB[i], m::mul(R(2), sb));
+            }
+            sl.publish(KB, k0);
+            pk_block_sync();
+            if constexpr (STEP_ACC) sl.vjp(Y2, r2, KB, k0, ub, YB, pst);
+            else sl.vjp(Y2, r2, KB, k0, ub, YB, PB);
+#pragma unroll
+            for (int i = 0; i < MM; ++i) {
+                const R sb = m::mul(a.h6, LAM[i]);
+                QB[i] = m::add(QB[i], YB[i]);
+                KB[i] = m::fma(a.h2, YB[i], sb);
+            }
+            sl.publish(KB, k1);
+            pk_block_sync();
+            if constexpr (STEP_ACC) sl.vjp(QC, rq, KB, k1, ua, YB, pst);
+            else sl.vjp(QC, rq, KB, k1, ua, YB, PB);
+#pragma unroll
+            for (int i = 0; i < MM; ++i) { LAM[i] = m::add(QB[i], YB[i]); QN[i] = QC[i]; }
+            if constexpr (STEP_ACC) {
+                if (valid) sl.add_pbar(pst, a.pbar, B, b);
+#pragma unroll
+                for (int p = 0; p < PO; ++p) pst[p] = R(0);
+            }
+            pk_block_sync();   // every slice is done with this step's regions
+        }
+    }
+    if (!valid) return;
+    sl.store_vec(LAM, a.dx0, B, b);
+    if constexpr (!STEP_ACC) sl.store_pbar(PB, a.pbar, B, b);
+}
+
 }  // namespace pk

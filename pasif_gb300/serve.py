@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import time
 
 import numpy as np
@@ -22,7 +23,7 @@ from . import synth
 
 
 def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, capacity=16384,
-        arena_samples=1 << 25, adjoint_budget=16 << 30, adjoint_workers=3, check=6, log=None) -> dict:
+        arena_samples=1 << 25, adjoint_budget=32 << 30, adjoint_workers=16, check=6, log=None) -> dict:
     dofs = tuple(dofs or synth.SERVED_DOFS)
     specs = S.served_specs(dofs)
     stream = synth.served_stream(rate, duration, seed, dofs=dofs)
@@ -98,6 +99,7 @@ def _rel(a, b) -> float:
 
 
 def main():
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")   # pools and adjoint workers on their own queues
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=1.5)

@@ -44,7 +44,10 @@ class Pool:
     """Serving pool of one pattern class (pasif_pool_* of the C ABI)."""
 
     def __init__(self, pattern: Pattern, precision="fp32_kahan", window: int = 0, im=None, h: float = 1e-3,
-                 max_comp=(), sq_comp=(), capacity: int = 4096, arena_samples: int = 1 << 22, chunk: int = 1024):
+                 max_comp=(), sq_comp=(), capacity: int = 4096, arena_samples: int = 1 << 22, chunk: int = 1024,
+                 slicing=None):
+        """slicing: None = by state size, True = warp-sliced kernel, False =
+        thread per system."""
         self.pattern = pattern
         self.capacity = int(capacity)
         self.arena_samples = int(arena_samples)
@@ -57,9 +60,10 @@ class Pool:
         w = N.f64(im).reshape(-1) if (window and im is not None) else None
         red = reducers_c(self.max_comp, 0, self.sq_comp, 0)
         hdl = C.c_void_p()
+        flags = 0 if slicing is None else (N.PLAN_WARP_SLICED if slicing else N.PLAN_NO_WARP_SLICED)
         N.check(N.lib.pasif_pool_create(C.byref(hdl), C.byref(self._c), prec, int(window),
                                         N.dptr(w) if w is not None else None, self.h, C.byref(red), self.capacity,
-                                        self.arena_samples, self.chunk))
+                                        self.arena_samples, self.chunk, flags))
         self.handle = hdl
         self._fin = np.zeros(self.capacity, np.int32)
 

@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <barrier>
+#include <thread>
 #include <vector>
 
 #define __device__
@@ -28,7 +30,50 @@ static inline float __fsub_rn(float a, float b) { return a - b; }
 using std::fabs;
 using std::fmax;
 struct EmuDim { unsigned x, y, z; };
-static EmuDim blockIdx, threadIdx, blockDim;
+static thread_local EmuDim blockIdx, threadIdx;
+static EmuDim blockDim;
+
+// Warp-sliced kernels: the L warps of a system run as L host threads sharing
+// that system's shared-memory buffers, the CTA barrier is a std::barrier.
+#define PK_HOST_EMU 1
+static thread_local unsigned char* emu_smem = nullptr;
+static thread_local std::barrier<>* emu_bar = nullptr;
+static inline unsigned char* pk_dyn_smem() { return emu_smem; }
+static inline void pk_block_sync() {
+    if (emu_bar) emu_bar->arrive_and_wait();
+}
+static inline unsigned pk_warp_max(unsigned v) { return v; }   // one system per emulated block
+
+static int emu_ws_slices() {
+    const char* s = std::getenv("EMU_WS_L");
+    return s ? std::atoi(s) : 0;
+}
+
+// Run `call` for system b: one thread per thread-per-system kernel, L barrier-
+// synchronised threads for a warp-sliced one (EMU_WS_L, EMU_WS_SMEM bytes).
+template <class F>
+static void emu_launch(long long b, F&& call) {
+    const int L = emu_ws_slices();
+    if (L <= 0) {
+        blockIdx.x = (unsigned)(b / 128);
+        threadIdx.x = (unsigned)(b % 128);
+        call();
+        return;
+    }
+    const char* sz = std::getenv("EMU_WS_SMEM");
+    std::vector<unsigned char> sm((sz ? std::atoll(sz) : 0) + 64, 0);
+    std::barrier<> bar(L);
+    std::vector<std::thread> th;
+    for (int w = 0; w < L; ++w)
+        th.emplace_back([&, w] {
+            emu_smem = sm.data();
+            emu_bar = &bar;
+            blockIdx.x = (unsigned)(b / 32);
+            threadIdx.x = (unsigned)(w * 32 + b % 32);
+            call();
+        });
+    for (auto& t : th) t.join();
+}
 
 #include GEN_SOURCE
 
@@ -135,9 +180,7 @@ int main(int argc, char** argv) {
             sstart[b] = (int)q[7];
         }
         for (int b = 0; b < C; ++b) {
-            blockIdx.x = (unsigned)(b / 128);
-            threadIdx.x = (unsigned)(b % 128);
-            pk_pool(p);
+            emu_launch(b, [&] { pk_pool(p); });
         }
     }
     for (int j = 0; j < J; ++j)
@@ -194,11 +237,7 @@ int main(int argc, char** argv) {
     a.B = B;
     a.step0 = step0;
     a.nsteps = nsteps;
-    for (int b = 0; b < B; ++b) {
-        blockIdx.x = (unsigned)(b / 128);
-        threadIdx.x = (unsigned)(b % 128);
-        pk_fwd(a);
-    }
+    for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_fwd(a); });
     std::snprintf(path, sizeof path, "%s/out.bin", dir);
     FILE* f = std::fopen(path, "wb");
     std::fwrite(state.data(), sizeof(R), state.size(), f);
@@ -234,11 +273,7 @@ int main(int argc, char** argv) {
     a.nck = nck;
     a.kahan = kahan;
     a.sq_start = sq_start;
-    for (int b = 0; b < B; ++b) {
-        blockIdx.x = (unsigned)(b / 128);
-        threadIdx.x = (unsigned)(b % 128);
-        pk_adj(a);
-    }
+    for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_adj(a); });
     std::snprintf(path, sizeof path, "%s/pbar.bin", dir);
     FILE* f = std::fopen(path, "wb");
     std::fwrite(pbar.data(), sizeof(double), pbar.size(), f);

@@ -62,3 +62,44 @@ def test_adjoint_config3_fd_and_fp32(gpu):
     dv32, _ = gpu_adjoint(*args, "fp32_kahan", None, gs, w.sq_comp, w.sq_start)
     rel = np.abs(dv32 - dv) / (np.abs(dv) + 1e-3 * np.abs(dv).max())
     assert rel.max() < 1e-4
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_adjoint_warp_sliced_fp64(gpu, seed):
+    """Warp-sliced adjoint (gather-form VJP across warps) forced on small
+    random patterns, batch not a multiple of 32: equal to the oracle bit for
+    bit in FP64."""
+    rng = np.random.default_rng(310 + seed)
+    pat, v = cases.random_system(rng, n=[3, 5, 8][seed])
+    B = 45
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    x = cases.signals(rng, 2, 120)
+    exc = rng.integers(0, 2, B)
+    N = [50, 97, 144][seed]
+    gf = rng.normal(size=(B, pat.n))
+    gs = rng.normal(size=B)
+    sq = (0, pat.n - 1)
+    plan = Plan(pat, "fp64", slicing=True)
+    b = Batch(plan, vals, x0, exc)
+    im = [[0, .5], [1, .5]]
+    dv, dx = b.adjoint(Signals(x, 2, im, "fp64"), 0.03, N, g_final=gf, g_sq=gs, sq_comp=sq, sq_start=N // 3)
+    assert b.kernel_info()["adjoint"] == "specialised"
+    odv, odx = O.batch_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, im, gf, gs, sq, N // 3)
+    np.testing.assert_array_equal(dv, odv)
+    np.testing.assert_array_equal(dx, odx)
+
+
+@pytest.mark.parametrize("nd", [4, 16, 32])
+def test_adjoint_warp_sliced_fp32_equals_thread(gpu, nd):
+    """FP32-Kahan adjoint of spring chains: warp-sliced and thread-per-system
+    kernels give the same bits (same per-step FP32 sums, same FP64 totals)."""
+    w = synth.chain8(n_sys=50, nsteps=300, nd=nd)
+    out = []
+    for slicing in (True, False):
+        plan = Plan(w.pattern, "fp32_kahan", slicing=slicing)
+        b = Batch(plan, w.values, w.x0, w.exc_index)
+        out.append(b.adjoint(Signals(w.signals, w.window, w.im, "fp32_kahan"), w.h, w.nsteps,
+                             g_sq=np.ones(w.n_sys), sq_comp=tuple(range(nd)), sq_start=w.nsteps // 2))
+        assert b.kernel_info()["adjoint"] == "specialised"
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])

@@ -128,3 +128,53 @@ def test_config2_full_horizon_fp32_kahan_within_1e5(gpu):
     rel_p = np.abs(res["fp32"] - res["fp64"]) / np.abs(res["fp64"])
     assert rel_k.max() <= 1e-5, rel_k.max()
     assert rel_p.max() > rel_k.max()   # the compensation is what buys the bound
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("seed", range(4))
+def test_forward_warp_sliced_bit_exact(gpu, prec, seed):
+    """Warp-sliced kernel (several warps per 32 systems, components crossing
+    warps through shared memory) forced on small random patterns, with a
+    batch that is not a multiple of 32: equal to the oracle bit for bit."""
+    rng = np.random.default_rng(300 + seed)
+    pat, v = cases.random_system(rng)
+    if pat.n < 2:
+        pytest.skip("one component: nothing to slice")
+    B, E, L = 83, 3, 90
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    x = cases.signals(rng, E, L)
+    exc = rng.integers(0, E, B)
+    W = [0, 2, 8, 4][seed]
+    im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
+    red = dict(max_comp=[0], max_start=40, sq_comp=sorted({0, pat.n - 1}), sq_start=10)
+    step0 = [0, 3, 0, 17][seed]
+    N = 120
+    plan = Plan(pat, prec, slicing=True)
+    b = Batch(plan, vals, x0, exc)
+    b.forward(Signals(x, W, im, prec), 0.05, N, step0=step0, **red)
+    st, mx, sq = b.get()
+    assert b.kernel_info()["kind"] == "specialised"
+    ost, omx, osq = O.batch_forward(pat, vals, x0, exc, x, 0.05, N, W, im, prec, step0, **red)
+    np.testing.assert_array_equal(st, ost)
+    np.testing.assert_array_equal(mx, omx)
+    np.testing.assert_array_equal(sq, osq)
+
+
+@pytest.mark.parametrize("nd", [14, 32, 64])
+def test_forward_warp_sliced_chain(gpu, nd):
+    """Spring chains of 28, 64 and 128 states (warp-sliced by default) with
+    trajectory output: equal to the thread-per-system kernel and the oracle."""
+    w = synth.chain8(n_sys=70, nsteps=400, nd=nd)
+    red = dict(max_comp=list(range(min(nd, 8))), max_start=100, sq_comp=list(range(min(nd, 64))), sq_start=200)
+    out = {}
+    for slicing in (None, False):
+        plan = Plan(w.pattern, "fp32_kahan", slicing=slicing)
+        b = Batch(plan, w.values, w.x0, w.exc_index)
+        b.forward(Signals(w.signals, w.window, w.im, "fp32_kahan"), w.h, w.nsteps, **red)
+        out[slicing] = b.get()
+    ost, omx, osq = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
+                                    "fp32_kahan", 0, **red)
+    for got in out.values():
+        np.testing.assert_array_equal(got[0], ost)
+        np.testing.assert_array_equal(got[1], omx)
+        np.testing.assert_array_equal(got[2], osq)

@@ -23,14 +23,18 @@ def alone(pat, prec, vals, x0, exc, x, W, im, h, N, max_comp, ms, sq_comp, ss):
     return b.get()
 
 
+@pytest.mark.parametrize("slicing", [False, True])
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
 @pytest.mark.parametrize("seed,W", [(0, 4), (1, 0), (2, 8)])
-def test_pool_requests_equal_alone(gpu, prec, seed, W):
+def test_pool_requests_equal_alone(gpu, prec, seed, W, slicing):
     rng = np.random.default_rng(1100 + seed)
     pat, v = cases.random_system(rng)
+    if slicing and pat.n < 2:
+        pytest.skip("one component: nothing to slice")
     im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
     max_comp, sq_comp, h = (0,), sorted({0, pat.n - 1}), 0.05
-    pool = S.Pool(pat, prec, W, im, h, max_comp, sq_comp, capacity=40, arena_samples=4000, chunk=23)
+    pool = S.Pool(pat, prec, W, im, h, max_comp, sq_comp, capacity=40, arena_samples=4000, chunk=23,
+                  slicing=slicing)
     reqs, live, done = [], {}, {}
     for j in range(12):
         m = int(rng.integers(1, 12))

@@ -5,6 +5,7 @@ oracle bit for bit.  Covers the interval loop (prologue, whole intervals,
 epilogue), the literal folding and the canonical accumulation order without
 a GPU."""
 import os
+import re
 import shutil
 import subprocess
 
@@ -20,17 +21,32 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(os.path.dirname(HERE), "pasif_gb300", "csrc")
 
 
-def run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, h, step0, nsteps, prec):
+def build_emulator(d, src, define=None):
+    """Compile a generated kernel source with the host harness; returns the
+    executable and the environment that selects its launch shape."""
     if shutil.which("g++") is None:
         pytest.skip("no host C++ compiler")
-    src = Plan(pat, prec).jit_report(vals, window=W, im=im).split("// ---- source ----\n", 1)[1]
-    d = str(tmp_path)
     open(os.path.join(d, "gen.cu"), "w").write(src)
     exe = os.path.join(d, "emu")
-    r = subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", f"-DGEN_SOURCE=\"gen.cu\"", "-I", CSRC,
-                        "-I", d, os.path.join(HERE, "hostemu", "emu_main.cpp"), "-o", exe],
-                       capture_output=True, text=True)
+    cmd = ["g++", "-O1", "-std=c++20", "-pthread", "-ffp-contract=off", f"-DGEN_SOURCE=\"gen.cu\"", "-I", CSRC,
+           "-I", d, os.path.join(HERE, "hostemu", "emu_main.cpp"), "-o", exe]
+    if define:
+        cmd.insert(1, f"-D{define}")
+    r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+    env = dict(os.environ)
+    m = re.search(r"// ws-launch (\d+) (\d+)", src)
+    if m:
+        env["EMU_WS_L"] = str(int(m.group(1)) // 32)
+        env["EMU_WS_SMEM"] = m.group(2)
+    return exe, env
+
+
+def run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, h, step0, nsteps, prec, slicing=None):
+    src = Plan(pat, prec, slicing=slicing).jit_report(vals, window=W, im=im).split("// ---- source ----\n", 1)[1]
+    assert ("warp-sliced" in src) == (bool(slicing) or (slicing is None and pat.n >= 28))
+    d = str(tmp_path)
+    exe, env = build_emulator(d, src)
     dt = np.float64 if prec == "fp64" else np.float32
     B = vals.shape[0]
     np.ascontiguousarray(vals.T.astype(dt)).tofile(os.path.join(d, "vals.bin"))
@@ -40,14 +56,15 @@ def run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, h, step0, nsteps, prec)
     (np.asarray(im, dt).reshape(-1) if W else np.zeros(0, dt)).tofile(os.path.join(d, "im.bin"))
     xs = np.asarray(x)
     r = subprocess.run([exe, d, str(B), str(pat.n), str(pat.P), str(xs.shape[0]), str(xs.shape[1]), str(W),
-                        str(step0), str(nsteps), repr(float(h)), "0"], capture_output=True, text=True)
+                        str(step0), str(nsteps), repr(float(h)), "0"], capture_output=True, text=True, env=env)
     assert r.returncode == 0, r.stderr
     return np.fromfile(os.path.join(d, "out.bin"), dtype=dt).reshape(pat.n, B).T.astype(np.float64)
 
 
+@pytest.mark.parametrize("slicing", [False, True])
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
 @pytest.mark.parametrize("seed,W,step0,nsteps", [(0, 8, 3, 61), (1, 0, 0, 40), (2, 4, 1, 30), (3, 2, 0, 25)])
-def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps):
+def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps, slicing):
     rng = np.random.default_rng(500 + seed)
     pat, v = cases.random_system(rng)
     B = 40
@@ -55,53 +72,81 @@ def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps)
     x = cases.signals(rng, 3, 28)   # shorter than the run: exercises the gating
     exc = rng.integers(0, 3, B)
     im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
-    got = run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, 0.05, step0, nsteps, prec)
+    if slicing and pat.n < 2:
+        pytest.skip("one component: nothing to slice")
+    got = run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, 0.05, step0, nsteps, prec, slicing)
     ref, _, _ = O.batch_forward(pat, vals, x0, exc, x, 0.05, nsteps, W, im, prec, step0)
     np.testing.assert_array_equal(got, ref)
 
 
-@pytest.mark.parametrize("seed", range(3))
-def test_generated_adjoint_matches_oracle(tmp_path, seed):
-    """FP64 specialised adjoint (registers + FP64 gradient totals) equals the
-    oracle's exact discrete adjoint bit for bit."""
-    if shutil.which("g++") is None:
-        pytest.skip("no host C++ compiler")
+def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, sq_start, h=0.03):
+    mask = sum(1 << c for c in sq)
+    src = Plan(pat, prec, slicing=slicing).jit_report_adjoint(vals, sq_mask=mask)
+    src = src.split("// ---- source ----\n", 1)[1]
+    assert ("warp-sliced" in src) == bool(slicing)
+    exe, env = build_emulator(d, src, "EMU_ADJ")
+    dt = np.float64 if prec == "fp64" else np.float32
+    B = len(vals)
+    np.ascontiguousarray(vals.T, dt).tofile(os.path.join(d, "vals.bin"))
+    np.ascontiguousarray(x0.T, dt).tofile(os.path.join(d, "x0.bin"))
+    np.asarray(exc, np.int32).tofile(os.path.join(d, "exc.bin"))
+    np.asarray(x, dt).tofile(os.path.join(d, "x.bin"))
+    np.ascontiguousarray(gs, dt).tofile(os.path.join(d, "gsq.bin"))
+    np.ascontiguousarray(gf.T, dt).tofile(os.path.join(d, "gfin.bin"))
+    np.asarray(im, dt).tofile(os.path.join(d, "im.bin"))
+    r = subprocess.run([exe, d, str(B), str(pat.n), str(pat.P), str(x.shape[0]), str(x.shape[1]), str(im.shape[1]),
+                        "0", str(N), repr(h), "1" if prec == "fp32_kahan" else "0", str(sq_start)],
+                       capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stderr
+    pbar = np.fromfile(os.path.join(d, "pbar.bin")).reshape(pat.P, B).T
+    dx0 = np.fromfile(os.path.join(d, "dx0.bin"), dtype=dt).reshape(pat.n, B).T.astype(np.float64)
+    return pbar, dx0
+
+
+def _adjoint_case(seed):
     rng = np.random.default_rng(700 + seed)
-    pat, v = cases.random_system(rng)
+    pat, v = cases.random_system(rng, n=[2, 5, 7][seed])
     B = 24
     vals, x0 = cases.random_batch(rng, pat, v, B)
     x = cases.signals(rng, 2, 90)
     exc = rng.integers(0, 2, B)
     N = [37, 64, 101][seed]
     sq = (0,) if pat.n == 1 else (0, pat.n - 1)
-    mask = sum(1 << c for c in sq)
     gf = rng.normal(size=(B, pat.n))
     gs = rng.normal(size=B)
-    src = Plan(pat, "fp64").jit_report_adjoint(vals, sq_mask=mask).split("// ---- source ----\n", 1)[1]
-    d = str(tmp_path)
-    open(os.path.join(d, "gen.cu"), "w").write(src)
-    exe = os.path.join(d, "emu")
-    r = subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-DEMU_ADJ", f"-DGEN_SOURCE=\"gen.cu\"",
-                        "-I", CSRC, "-I", d, os.path.join(HERE, "hostemu", "emu_main.cpp"), "-o", exe],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-3000:]
-    np.ascontiguousarray(vals.T).tofile(os.path.join(d, "vals.bin"))
-    np.ascontiguousarray(x0.T).tofile(os.path.join(d, "x0.bin"))
-    np.asarray(exc, np.int32).tofile(os.path.join(d, "exc.bin"))
-    np.asarray(x, np.float64).tofile(os.path.join(d, "x.bin"))
-    np.zeros(2 * 2).tofile(os.path.join(d, "im.bin"))
-    np.ascontiguousarray(gs).tofile(os.path.join(d, "gsq.bin"))
-    np.ascontiguousarray(gf.T).tofile(os.path.join(d, "gfin.bin"))
     im = np.array([[0, .5], [1, .5]])
-    im.tofile(os.path.join(d, "im.bin"))
-    r = subprocess.run([exe, d, str(B), str(pat.n), str(pat.P), "2", "90", "2", "0", str(N), repr(0.03), "0",
-                        str(N // 3)], capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
-    pbar = np.fromfile(os.path.join(d, "pbar.bin")).reshape(pat.P, B).T
-    dx0 = np.fromfile(os.path.join(d, "dx0.bin")).reshape(pat.n, B).T
+    return pat, vals, x0, exc, x, im, gf, gs, N, sq
+
+
+@pytest.mark.parametrize("slicing", [False, True])
+@pytest.mark.parametrize("seed", range(3))
+def test_generated_adjoint_matches_oracle(tmp_path, seed, slicing):
+    """FP64 specialised adjoint (registers + FP64 gradient totals; thread per
+    system or warp-sliced with the gather-form VJP) equals the oracle's exact
+    discrete adjoint bit for bit."""
+    pat, vals, x0, exc, x, im, gf, gs, N, sq = _adjoint_case(seed)
+    if slicing and pat.n < 2:
+        pytest.skip("one component: nothing to slice")
+    pbar, dx0 = run_emulated_adjoint(str(tmp_path), pat, "fp64", slicing, vals, x0, exc, x, im, gf, gs, N, sq, N // 3)
     odv, odx = O.batch_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, im, gf, gs, sq, N // 3)
     np.testing.assert_array_equal(pbar, odv)
     np.testing.assert_array_equal(dx0, odx)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_generated_adjoint_fp32_sliced_equals_thread(tmp_path, seed):
+    """FP32 adjoint (per-step FP32 gradient sums into FP64 totals): the warp-
+    sliced kernel equals the thread-per-system kernel bit for bit."""
+    pat, vals, x0, exc, x, im, gf, gs, N, sq = _adjoint_case(seed)
+    if pat.n < 2:
+        pytest.skip("one component: nothing to slice")
+    out = []
+    for slicing in (False, True):
+        d = os.path.join(str(tmp_path), str(slicing))
+        os.makedirs(d)
+        out.append(run_emulated_adjoint(d, pat, "fp32_kahan", slicing, vals, x0, exc, x, im, gf, gs, N, sq, N // 3))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
 
 
 def test_generated_kernel_config2(tmp_path):
@@ -132,9 +177,10 @@ def _pool_jobs(rng, pat, v, C, W):
     return jobs
 
 
+@pytest.mark.parametrize("slicing", [False, True])
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
 @pytest.mark.parametrize("seed,W", [(0, 4), (1, 0), (2, 2)])
-def test_generated_pool_matches_oracle(tmp_path, prec, seed, W):
+def test_generated_pool_matches_oracle(tmp_path, prec, seed, W, slicing):
     """Serving-pool chunk kernel: every system of every job, run in 16-step
     chunks beside other jobs that join and leave, equals the oracle run of
     that job alone, bit for bit (state, max and sum-of-squares reducers)."""
@@ -147,14 +193,13 @@ def test_generated_pool_matches_oracle(tmp_path, prec, seed, W):
     im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
     max_comp = (0,)
     sq_comp = (0,) if pat.n == 1 else (0, pat.n - 1)
-    src = Plan(pat, prec).jit_report_pool(W, im, max_comp, sq_comp).split("// ---- source ----\n", 1)[1]
+    if slicing and pat.n < 2:
+        pytest.skip("one component: nothing to slice")
+    src = Plan(pat, prec, slicing=slicing).jit_report_pool(W, im, max_comp, sq_comp)
+    src = src.split("// ---- source ----\n", 1)[1]
+    assert ("warp-sliced" in src) == slicing
     d = str(tmp_path)
-    open(os.path.join(d, "gen.cu"), "w").write(src)
-    exe = os.path.join(d, "emu")
-    r = subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-DEMU_POOL", f"-DGEN_SOURCE=\"gen.cu\"",
-                        "-I", CSRC, "-I", d, os.path.join(HERE, "hostemu", "emu_main.cpp"), "-o", exe],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-3000:]
+    exe, env = build_emulator(d, src, "EMU_POOL")
     dt = np.float64 if prec == "fp64" else np.float32
     rows, tab, vals, x0, arena, off = [], [], [], [], [], 0
     for jb in jobs:
@@ -174,7 +219,7 @@ def test_generated_pool_matches_oracle(tmp_path, prec, seed, W):
     np.concatenate(arena).astype(dt).tofile(os.path.join(d, "arena.bin"))
     (np.asarray(im, dt).reshape(-1) if W else np.zeros(0, dt)).tofile(os.path.join(d, "im.bin"))
     r = subprocess.run([exe, d, str(C), str(pat.n), str(pat.P), str(off), str(W), str(chunk), repr(0.05),
-                        str(len(rows)), str(T)], capture_output=True, text=True)
+                        str(len(rows)), str(T)], capture_output=True, text=True, env=env)
     assert r.returncode == 0, r.stderr
     J = len(rows)
     st = np.fromfile(os.path.join(d, "state.bin"), dtype=dt).reshape(J, pat.n).astype(np.float64)
@@ -189,3 +234,15 @@ def test_generated_pool_matches_oracle(tmp_path, prec, seed, W):
         np.testing.assert_array_equal(mx[k:k + m, list(max_comp)], omx)
         np.testing.assert_array_equal(sq[k:k + m], osq)
         k += m
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
+def test_generated_warp_sliced_banded32(tmp_path, prec):
+    """64-state banded system: the default kernel is warp-sliced (8 warps,
+    components crossing warps through shared memory); equals the oracle."""
+    w = synth.banded32(n_sys=6, nsteps=150, sig_len=256)
+    got = run_emulated(tmp_path, w.pattern, w.values, w.x0, w.exc_index, w.signals, w.window, w.im, w.h, 0,
+                       w.nsteps, prec, slicing=None if prec == "fp32_kahan" else True)
+    ref, _, _ = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
+                                prec)
+    np.testing.assert_array_equal(got, ref)

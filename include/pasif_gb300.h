@@ -189,9 +189,17 @@ int pasif_plan_destroy(pasif_plan* p);
 int pasif_signals_create(pasif_signals** out, const double* x, int n_exc, int len, int window,
                          const double* im, int precision, int memory, void* stream);
 int pasif_signals_destroy(pasif_signals* s);
+/* Replace the table (same window, weights and precision) in the existing
+ * device buffers, grown only when too small: no device allocation, hence no
+ * implicit device synchronisation, once they are large enough.  No reference
+ * counterpart (serving workers reuse one table object). */
+int pasif_signals_update(pasif_signals* s, const double* x, int n_exc, int len, int memory, void* stream);
 
 int pasif_batch_create(pasif_batch** out, pasif_plan* plan, int n_sys);
 int pasif_batch_destroy(pasif_batch* b);
+/* New instance count for the next pasif_batch_set; device buffers are kept
+ * and grown only when too small (a batch reused across requests). */
+int pasif_batch_resize(pasif_batch* b, int n_sys);
 /* values[n_sys][P], x0[n_sys][n], exc_index[n_sys]. */
 int pasif_batch_set(pasif_batch* b, const double* values, const double* x0, const int* exc_index,
                     int memory, void* stream);

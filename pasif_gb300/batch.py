@@ -104,6 +104,16 @@ class Signals:
                                            _stream(stream)))
         self.handle = h
 
+    def update(self, x, stream=None):
+        """New table (same window, weights, precision) in the existing device
+        buffers: no allocation once they are large enough."""
+        x = N.f64(x)
+        if x.ndim == 1:
+            x = x[None, :]
+        N.check(N.lib.pasif_signals_update(self.handle, C.c_void_p(x.ctypes.data), x.shape[0], x.shape[1], N.HOST,
+                                           _stream(stream)))
+        self.n_exc, self.len = x.shape
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h:
@@ -126,7 +136,13 @@ class Batch:
         self.set(values, x0, exc_index, stream)
 
     def set(self, values, x0, exc_index, stream=None):
+        """New inputs; a different instance count resizes the batch (its
+        device buffers are kept, and grown only when too small)."""
         p = self.plan.pattern
+        m = int(len(exc_index))
+        if m != self.n_sys:
+            N.check(N.lib.pasif_batch_resize(self.handle, m))
+            self.n_sys = m
         if _is_device(values):
             mem = N.DEVICE
             ptrs = [C.c_void_p(t.data_ptr()) for t in (values, x0, exc_index)]

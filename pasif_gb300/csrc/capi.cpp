@@ -338,6 +338,20 @@ int pasif_signals_destroy(pasif_signals* s) {
     return PASIF_OK;
 }
 
+int pasif_signals_update(pasif_signals* s, const double* x, int n_exc, int len, int memory, void* stream) {
+    if (!s || !s->s) return fail(PASIF_ERR_INVALID, "null signals");
+    return guard([&] {
+        std::string err;
+        return done(pasif::signals_update(*s->s, x, n_exc, len, memory, (cudaStream_t)stream, &err), err);
+    });
+}
+
+int pasif_batch_resize(pasif_batch* b, int n_sys) {
+    if (!b || !b->b) return fail(PASIF_ERR_INVALID, "null batch");
+    std::string err;
+    return done(b->b->resize(n_sys, &err), err);
+}
+
 int pasif_batch_create(pasif_batch** out, pasif_plan* plan, int n_sys) {
     return guard([&] {
         if (!out || !plan) return fail(PASIF_ERR_INVALID, "null handle");
@@ -540,7 +554,7 @@ int pasif_plan_jit_report_adjoint(const pasif_plan* p, const double* values, int
         const bool f32 = p->p->precision != pasif::kFP64;
         const std::string src =
             pasif::adj_source(p->p->pat, literals_of(p->p->pat, f32, values, n_sys), f32, sq_mask,
-                              p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0),
+                              p->p->slicing < 0 ? 0 : pasif::ws_slices_adjoint(p->p->pat, f32, p->p->slicing > 0),
                               p->p->precision == pasif::kFP32Kahan);
         std::string report, err;
         if (!pasif::compile_report(src, &report, &err)) return fail(PASIF_ERR_NVRTC, err);

@@ -136,6 +136,24 @@ int signals_create(const double* x, int n_exc, int len, int window, const double
     return 0;
 }
 
+int signals_update(Signals& s, const double* x, int n_exc, int len, int memory, cudaStream_t st, std::string* err) {
+    if (n_exc < 1 || len < 1 || !x) { *err = "excitation table must hold at least one sample of one signal"; return 1; }
+    int rc = upload_conv(x, (long long)n_exc * len, s.f32, memory, s.x, s.stage, st, err);
+    if (rc) return rc;
+    s.n_exc = n_exc;
+    s.len = len;
+    PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    return 0;
+}
+
+int Batch::resize(int n_sys, std::string* err) {
+    if (n_sys < 0) { *err = "negative number of systems"; return 1; }
+    B = n_sys;
+    max_exc_ = -1;
+    last_kind = last_adj_kind = kNone;
+    return 0;
+}
+
 pk::GenPattern Plan::gen() const {
     pk::GenPattern g;
     g.data = gpat.as<int>();
@@ -440,7 +458,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     a.sq_mask = g_sq ? sm : 0ull;
     JitKernel jk;
     std::string jerr;
-    const int slices = plan->slicing < 0 ? 0 : ws_slices(pat, f, plan->slicing > 0);
+    const int slices = plan->slicing < 0 ? 0 : ws_slices_adjoint(pat, f, plan->slicing > 0);
     const bool jit = !plan->generic_only &&
                      get_adj_kernel(pat, lit, f, plan->precision == kFP32Kahan, g_sq ? sm : 0ull, slices, &jk, &jerr);
     if (!jit && !plan->generic_only) last_jit_error = jerr;

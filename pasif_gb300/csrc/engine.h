@@ -38,6 +38,7 @@ struct Signals {
     int len = 0;
     unsigned w = 0, lw = 0;
     DevBuf x, im;
+    DevBuf stage;                  // host-format staging of signals_update
     std::vector<double> im_host;   // the 2W weights rounded to the compute precision
     template <typename R> pk::Forcing<R> forcing() const {
         pk::Forcing<R> f;
@@ -55,6 +56,9 @@ struct Signals {
 // Build a signal table; x and im are host or device (memory) pointers.
 int signals_create(const double* x, int n_exc, int len, int window, const double* im, int precision,
                    int memory, cudaStream_t st, std::shared_ptr<Signals>* out, std::string* err);
+// New table of the same window / weights / precision in the existing device
+// buffers (grown when needed): no allocation once they are large enough.
+int signals_update(Signals& s, const double* x, int n_exc, int len, int memory, cudaStream_t st, std::string* err);
 
 struct Plan {
     Pattern pat;
@@ -96,6 +100,9 @@ struct Batch {
     bool f32() const { return plan->precision != kFP64; }
     size_t rsize() const { return f32() ? sizeof(float) : sizeof(double); }
 
+    // New instance count; the device buffers are kept and grown by the next
+    // set / solve when needed (a batch reused for requests of any size).
+    int resize(int n_sys, std::string* err);
     // values[B][P], x0[B][n] (double), exc_index[B]; host or device pointers.
     int set(const double* values, const double* x0h, const int* exc_index, int memory, cudaStream_t st,
             std::string* err);

@@ -820,6 +820,18 @@ int ws_slices(const Pattern& pat, bool f32, bool force) {
     const int n = pat.n;
     // measured crossover on GB300: thread per system wins below ~28 states in FP32, ~24 in FP64
     if (n < 2 || n > kWsMaxN || (!force && n < (f32 ? 28 : 24))) return 0;
+    return ws_split(n, f32, force);
+}
+
+int ws_slices_adjoint(const Pattern& pat, bool f32, bool force) {
+    const int n = pat.n;
+    // the adjoint keeps about twice the vectors of the forward: sliced from 12 states
+    // (16-state chain: 2x the thread-per-system gradient rate, 236 -> 150 registers)
+    if (n < 2 || n > kWsMaxN || (!force && n < 12)) return 0;
+    return ws_split(n, f32, force);
+}
+
+int ws_split(int n, bool f32, bool force) {
     const int cpw = force ? 2 : (f32 ? 8 : 6);   // components per warp
     const int L = (n + cpw - 1) / cpw;
     return std::max(2, std::min(16, std::min(L, n)));

@@ -101,7 +101,11 @@ int Pool::create(const Pattern& pat, int precision, int window, const double* im
     PL_CUDA(cudaMemset(p->remain_.p, 0, C * sizeof(int)), "cudaMemset");
     PL_CUDA(cudaMemset(p->vals_.p, 0, P * C * rs), "cudaMemset");
     PL_CUDA(cudaMemset(p->state_.p, 0, (size_t)n * C * rs), "cudaMemset");
-    PL_CUDA(cudaStreamCreateWithFlags(&p->st_, cudaStreamNonBlocking), "cudaStreamCreate");
+    // highest priority: a chunk's blocks are scheduled ahead of queued blocks of
+    // lower-priority work (e.g. adjoint sweeps), which bounds forward latency
+    int prio_least = 0, prio_greatest = 0;
+    PL_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest), "cudaDeviceGetStreamPriorityRange");
+    PL_CUDA(cudaStreamCreateWithPriority(&p->st_, cudaStreamNonBlocking, prio_greatest), "cudaStreamCreate");
     PL_CUDA(cudaMallocHost((void**)&p->remain_host_, C * sizeof(int)), "cudaMallocHost");
     p->free_.resize(C);
     for (int i = 0; i < capacity; ++i) p->free_[i] = capacity - 1 - i;   // pop_back gives ascending slots

@@ -214,6 +214,7 @@ class Server:
         self._threads = []
         self._n_adj_workers = int(adjoint_workers)
         self._plans = {}
+        self._tls = threading.local()     # per adjoint worker: reused batch and signal table per class
         self._errors = []
         self.t0 = self.clock()
         self.chunks = collections.Counter()
@@ -391,6 +392,10 @@ class Server:
                 self._cv.notify_all()
 
     def _run_adjoint(self, spec: ClassSpec, req: Request, stream):
+        """One adjoint request on this worker's stream.  Each worker keeps one
+        batch and one signal table per class and reuses their device buffers:
+        a device allocation or free per request would synchronise the whole
+        device and stall every other request in flight."""
         from .batch import Batch, Plan, Signals
         with self._cv:
             plan = self._plans.get(id(spec))
@@ -398,8 +403,16 @@ class Server:
             plan = Plan(spec.pattern, self.precision, literals=False)
             with self._cv:
                 plan = self._plans.setdefault(id(spec), plan)
-        sig = Signals(req.signals, spec.window, spec.im, self.precision, stream=stream)
-        b = Batch(plan, req.values, req.x0, req.exc_index, stream=stream)
+        cache = self._tls.__dict__.setdefault("objs", {})
+        objs = cache.get(id(spec))
+        if objs is None:
+            sig = Signals(req.signals, spec.window, spec.im, self.precision, stream=stream)
+            b = Batch(plan, req.values, req.x0, req.exc_index, stream=stream)
+            cache[id(spec)] = (sig, b)
+        else:
+            sig, b = objs
+            sig.update(req.signals, stream=stream)
+            b.set(req.values, req.x0, req.exc_index, stream=stream)
         return b.adjoint(sig, spec.h, req.nsteps, g_sq=np.ones(req.n_sys), sq_comp=spec.positions,
                          sq_start=req.sq_start, stream=stream)
 

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -310,10 +311,20 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
                                                   : (x.second.kind == 0 ? x.first < y.first : x.second.q < y.second.q);
         });
     }
+    // rolled stages when the slices are large (instruction cache), unrolled otherwise
+    size_t terms = 0;
+    for (const auto& t : dt) terms += t.size();
+    // Forward, 4 warps: 16-state chain slices of ~22 terms 1.4x faster unrolled;
+    // 32-, 64-state slices of 43-88 terms 1.2-2x faster rolled.  Adjoint (measured
+    // gradient rates): 16-state chain 1.2x faster unrolled, 32- and 64-state chains
+    // and the 64-state banded system 1.0-1.5x faster rolled, 128-state chain 1.35x
+    // faster unrolled.
+    bool roll = adj ? (n > 24 && n <= 96) : (double)terms / sl.L >= 30.0;
+    if (const char* e = std::getenv("PASIF_WS_ROLL")) roll = std::atoi(e) != 0;   // tuning override
     std::ostringstream o;
     o << "// generated by pasif_gb300 jit.cpp: warp-sliced "
       << (mode == 0 ? "forward" : mode == 1 ? "serving pool" : "exact adjoint") << " RK4, n=" << n
-      << " P=" << pat.P() << " slices=" << sl.L << " published=" << sl.NP << "\n";
+      << " P=" << pat.P() << " slices=" << sl.L << " published=" << sl.NP << " rolled=" << (roll ? 1 : 0) << "\n";
     o << "#include \"rk4_core.cuh\"\nnamespace pk {\n";
     o << "typedef " << (key.f32 ? "float" : "double") << " R;\n";
     for (int w = 0; w < sl.L; ++w) {
@@ -365,7 +376,8 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
         o << "  static constexpr int MM = " << MM << ", NP = " << sl.NP << ", PO = " << std::max<size_t>(pown.size(), 1)
           << ";\n";
         o << "  static constexpr bool FORCED = " << (forced ? "true" : "false")
-          << ", SQOWN = " << (w == sl.sq_owner ? "true" : "false") << ";\n";
+          << ", SQOWN = " << (w == sl.sq_owner ? "true" : "false") << ", ROLL = " << (roll ? "true" : "false")
+          << ";\n";
         o << "  R p[" << std::max<size_t>(slot.size(), 1) << "];\n";
         o << "  __device__ __forceinline__ void load(const R* __restrict__ vals, long long B, int b) {\n";
         for (auto& kv : slot) o << "    p[" << kv.second << "] = vals[" << kv.first << "LL * B + b];\n";
@@ -820,7 +832,7 @@ int ws_slices(const Pattern& pat, bool f32, bool force) {
     const int n = pat.n;
     // measured crossover on GB300: thread per system wins below ~28 states in FP32, ~24 in FP64
     if (n < 2 || n > kWsMaxN || (!force && n < (f32 ? 28 : 24))) return 0;
-    return ws_split(n, f32, force);
+    return ws_split(n, f32, force, false);
 }
 
 int ws_slices_adjoint(const Pattern& pat, bool f32, bool force) {
@@ -828,12 +840,22 @@ int ws_slices_adjoint(const Pattern& pat, bool f32, bool force) {
     // the adjoint keeps about twice the vectors of the forward: sliced from 12 states
     // (16-state chain: 2x the thread-per-system gradient rate, 236 -> 150 registers)
     if (n < 2 || n > kWsMaxN || (!force && n < 12)) return 0;
-    return ws_split(n, f32, force);
+    return ws_split(n, f32, force, true);
 }
 
-int ws_split(int n, bool f32, bool force) {
-    const int cpw = force ? 2 : (f32 ? 8 : 6);   // components per warp
-    const int L = (n + cpw - 1) / cpw;
+int ws_split(int n, bool f32, bool force, bool adjoint) {
+    // Forward: four warps when the registers allow (up to 32 FP32 / 16 FP64
+    // components per warp): each SM sub-partition then runs one slice's code.
+    // Measured on GB300 (forward, FP32-Kahan): 128-state chain 4 warps 1.86e9
+    // system-steps/s vs 8 warps 1.5e9, 16 warps 0.84e9; 64-state banded 1.68e9
+    // vs 1.30e9.  The adjoint holds about twice the vectors: 8 FP32 / 6 FP64
+    // components per warp, at least 4 and (FP32) at most 8 warps (gradient rates:
+    // 16-state chain 4 warps 1.32e9 vs 2 warps 1.01e9; 128-state chain 8 warps
+    // 1.35e8 vs 16 warps 0.98e8).
+    const int cpw = force ? 2 : adjoint ? (f32 ? 8 : 6) : (f32 ? 32 : 16);   // components per warp
+    int L = std::max(4, (n + cpw - 1) / cpw);
+    if (adjoint && f32 && !force) L = std::min(L, 8);
+    if (const char* e = std::getenv("PASIF_WS_SLICES")) L = std::atoi(e);   // tuning override
     return std::max(2, std::min(16, std::min(L, n)));
 }
 

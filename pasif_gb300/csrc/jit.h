@@ -45,7 +45,7 @@ int ws_slices(const Pattern& pat, bool f32, bool force);
 // Same for the exact adjoint (sliced from smaller systems).
 int ws_slices_adjoint(const Pattern& pat, bool f32, bool force);
 // Warps for n components (2..16).
-int ws_split(int n, bool f32, bool force);
+int ws_split(int n, bool f32, bool force, bool adjoint);
 
 // Source of the forward kernel for a pattern (exposed for tests and docs).
 std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key);

@@ -823,43 +823,52 @@ __device__ __forceinline__ unsigned pk_warp_max(unsigned v) { return __reduce_ma
 // One RK4 step of the slice (the operations of rk4_step): Q's foreign
 // components are read from b0, the stage vectors pass through b1 and b0, and
 // the new Q is published to b0.  act = false leaves Q and Cm unchanged.
+//
+// SL::ROLL: the four stages run as a rolled loop, so each slice's right-hand
+// side appears once in the code.  The warps of a block execute different
+// code; with large slices the unrolled stages of the warps sharing an SM
+// sub-partition overflow its instruction cache (fetch stalls dominated), with
+// small slices the unrolled form is faster (fewer instructions).
 template <typename R, bool KAHAN, class SL, class V>
 __device__ __forceinline__ void ws_step(const SL& sl, R* b0, R* b1, V& Q, V& Cm, V& S, V& K, V& Mi, R ua, R ub,
                                         R uc, R h, R h2, R h6, bool act) {
     typedef M<R> m;
     constexpr int MM = SL::MM;
-    sl.rhs(Q, b0, ua, K);
 #pragma unroll
-    for (int i = 0; i < MM; ++i) { S[i] = K[i]; Mi[i] = m::fma(h2, K[i], Q[i]); }
-    sl.publish(Mi, b1);
-    pk_block_sync();
-    sl.rhs(Mi, b1, ub, K);
+    for (int i = 0; i < MM; ++i) Mi[i] = Q[i];   // stage 1 evaluates at Q
+#pragma unroll(SL::ROLL ? 1 : 4)
+    for (int st = 0; st < 4; ++st) {
+        const R u = st == 0 ? ua : (st == 3 ? uc : ub);
+        sl.rhs(Mi, (st & 1) ? b1 : b0, u, K);
+        if (st == 3) {
 #pragma unroll
-    for (int i = 0; i < MM; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(h2, K[i], Q[i]); }
-    sl.publish(Mi, b0);
-    pk_block_sync();
-    sl.rhs(Mi, b0, ub, K);
-#pragma unroll
-    for (int i = 0; i < MM; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(h, K[i], Q[i]); }
-    sl.publish(Mi, b1);
-    pk_block_sync();
-    sl.rhs(Mi, b1, uc, K);
-#pragma unroll
-    for (int i = 0; i < MM; ++i) {
-        const R sum = m::add(S[i], K[i]);
-        if (KAHAN) {
-            const R inc = m::mul(h6, sum);
-            const R y = m::sub(inc, Cm[i]);
-            const R t = m::add(Q[i], y);
-            const R c = m::sub(m::sub(t, Q[i]), y);
-            if (act) { Cm[i] = c; Q[i] = t; }
+            for (int i = 0; i < MM; ++i) {
+                const R sum = m::add(S[i], K[i]);
+                if (KAHAN) {
+                    const R inc = m::mul(h6, sum);
+                    const R y = m::sub(inc, Cm[i]);
+                    const R t = m::add(Q[i], y);
+                    const R c = m::sub(m::sub(t, Q[i]), y);
+                    if (act) { Cm[i] = c; Q[i] = t; }
+                } else {
+                    const R t = m::fma(h6, sum, Q[i]);
+                    if (act) Q[i] = t;
+                }
+            }
+            sl.publish(Q, b0);
         } else {
-            const R t = m::fma(h6, sum, Q[i]);
-            if (act) Q[i] = t;
+            const R c = st == 2 ? h : h2;
+            if (st == 0) {
+#pragma unroll
+                for (int i = 0; i < MM; ++i) { S[i] = K[i]; Mi[i] = m::fma(c, K[i], Q[i]); }
+            } else {
+#pragma unroll
+                for (int i = 0; i < MM; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(c, K[i], Q[i]); }
+            }
+            sl.publish(Mi, (st & 1) ? b0 : b1);
         }
+        pk_block_sync();
     }
-    sl.publish(Q, b0);
-    pk_block_sync();
 }
 
 template <typename R, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, int N, class SL, class V>
@@ -1063,54 +1072,60 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             const R uc = force_at(a.frc, ebase, st, 1u, 0u);
             sl.publish(QC, rq);
             pk_block_sync();
-            sl.rhs(QC, rq, ua, K);
+            // stages: Y2 = QC + h/2 f(QC), Y3 = QC + h/2 f(Y2), Y4 = QC + h f(Y3), each
+            // published to its own region (rq, r2, r3, r4 follow each other); rolled
+            // like ws_step so that the right-hand side appears once in the code
+            V Yc;
 #pragma unroll
-            for (int i = 0; i < MM; ++i) Y2[i] = m::fma(a.h2, K[i], QC[i]);
-            sl.publish(Y2, r2);
-            pk_block_sync();
-            sl.rhs(Y2, r2, ub, K);
+            for (int i = 0; i < MM; ++i) Yc[i] = QC[i];
+#pragma unroll(SL::ROLL ? 1 : 3)
+            for (int st = 0; st < 3; ++st) {
+                sl.rhs(Yc, rq + st * NP * 32, st == 0 ? ua : ub, K);
+                const R c = st == 2 ? a.h : a.h2;
 #pragma unroll
-            for (int i = 0; i < MM; ++i) Y3[i] = m::fma(a.h2, K[i], QC[i]);
-            sl.publish(Y3, r3);
-            pk_block_sync();
-            sl.rhs(Y3, r3, ub, K);
+                for (int i = 0; i < MM; ++i) Yc[i] = m::fma(c, K[i], QC[i]);
+                if (st == 0) {
 #pragma unroll
-            for (int i = 0; i < MM; ++i) { Y4[i] = m::fma(a.h, K[i], QC[i]); KB[i] = m::mul(a.h6, LAM[i]); QB[i] = LAM[i]; }
-            sl.publish(Y4, r4);
-            sl.publish(KB, k0);
-            pk_block_sync();
-            if constexpr (STEP_ACC) sl.vjp(Y4, r4, KB, k0, uc, YB, pst);
-            else sl.vjp(Y4, r4, KB, k0, uc, YB, PB);
+                    for (int i = 0; i < MM; ++i) Y2[i] = Yc[i];
+                } else if (st == 1) {
 #pragma unroll
-            for (int i = 0; i < MM; ++i) {
-                const R sb = m::mul(a.h6, LAM[i]);
-                QB[i] = m::add(QB[i], YB[i]);
-                KB[i] = m::fma(a.h, YB[i], m::mul(R(2), sb));
+                    for (int i = 0; i < MM; ++i) Y3[i] = Yc[i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < MM; ++i) { Y4[i] = Yc[i]; KB[i] = m::mul(a.h6, LAM[i]); QB[i] = LAM[i]; }
+                    sl.publish(KB, k0);
+                }
+                sl.publish(Yc, rq + (st + 1) * NP * 32);
+                pk_block_sync();
             }
-            sl.publish(KB, k1);
-            pk_block_sync();
-            if constexpr (STEP_ACC) sl.vjp(Y3, r3, KB, k1, ub, YB, pst);
-            else sl.vjp(Y3, r3, KB, k1, ub, YB, PB);
+            // reverse sweep: VJPs at Y4, Y3, Y2, QC with weights from k0, k1, k0, k1
+#pragma unroll(SL::ROLL ? 1 : 4)
+            for (int st = 0; st < 4; ++st) {
+                if (st == 1) {
 #pragma unroll
-            for (int i = 0; i < MM; ++i) {
-                const R sb = m::mul(a.h6, LAM[i]);
-                QB[i] = m::add(QB[i], YB[i]);
-                KB[i] = m::fma(a.h2, YB[i], m::mul(R(2), sb));
-            }
-            sl.publish(KB, k0);
-            pk_block_sync();
-            if constexpr (STEP_ACC) sl.vjp(Y2, r2, KB, k0, ub, YB, pst);
-            else sl.vjp(Y2, r2, KB, k0, ub, YB, PB);
+                    for (int i = 0; i < MM; ++i) Yc[i] = Y3[i];
+                } else if (st == 2) {
 #pragma unroll
-            for (int i = 0; i < MM; ++i) {
-                const R sb = m::mul(a.h6, LAM[i]);
-                QB[i] = m::add(QB[i], YB[i]);
-                KB[i] = m::fma(a.h2, YB[i], sb);
+                    for (int i = 0; i < MM; ++i) Yc[i] = Y2[i];
+                } else if (st == 3) {
+#pragma unroll
+                    for (int i = 0; i < MM; ++i) Yc[i] = QC[i];
+                }   // st == 0: Yc holds Y4
+                const R u = st == 0 ? uc : (st == 3 ? ua : ub);
+                R* const yb = rq + (3 - st) * NP * 32;
+                if constexpr (STEP_ACC) sl.vjp(Yc, yb, KB, (st & 1) ? k1 : k0, u, YB, pst);
+                else sl.vjp(Yc, yb, KB, (st & 1) ? k1 : k0, u, YB, PB);
+                if (st == 3) break;
+                const R c = st == 0 ? a.h : a.h2;
+#pragma unroll
+                for (int i = 0; i < MM; ++i) {
+                    const R sb = m::mul(a.h6, LAM[i]);
+                    QB[i] = m::add(QB[i], YB[i]);
+                    KB[i] = m::fma(c, YB[i], st < 2 ? m::mul(R(2), sb) : sb);
+                }
+                sl.publish(KB, (st & 1) ? k0 : k1);
+                pk_block_sync();
             }
-            sl.publish(KB, k1);
-            pk_block_sync();
-            if constexpr (STEP_ACC) sl.vjp(QC, rq, KB, k1, ua, YB, pst);
-            else sl.vjp(QC, rq, KB, k1, ua, YB, PB);
 #pragma unroll
             for (int i = 0; i < MM; ++i) { LAM[i] = m::add(QB[i], YB[i]); QN[i] = QC[i]; }
             if constexpr (STEP_ACC) {

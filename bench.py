@@ -291,7 +291,9 @@ def main():
         adj[prec] = {"gradients_per_s": c3.n_sys / dt, "adjoint_system_steps_per_s": c3.n_sys * c3.nsteps / dt,
                      "seconds": dt, "kernel": bt.kernel_info()["adjoint"]}
     g32, g64 = grads["fp32_kahan"], grads["fp64"]
-    grel = np.abs(g32 - g64) / (np.abs(g64) + 1e-6 * np.abs(g64).max())
+    # per system: max |g32 - g64| over its 43 values / max |g64| (normwise; an
+    # elementwise ratio is meaningless for gradient entries that are ~0)
+    grel = np.max(np.abs(g32 - g64), axis=1) / np.maximum(np.max(np.abs(g64), axis=1), 1e-300)
 
     # served mixed stream: Poisson 200 req/s, 70/30 forward/adjoint, 1-4096
     # systems of DOF 1..64, 1e4-2e5 steps (continuous batching, p50/p99)
@@ -330,7 +332,9 @@ def main():
                                         "gradients w.r.t. all 43 values per system (wall time of the C-ABI call)",
                             "fp32_kahan": adj["fp32_kahan"], "fp64": adj["fp64"],
                             "max_rel_err_grad_fp32_kahan_vs_fp64": float(grel.max()),
-                            "median_rel_err_grad": float(np.median(grel))},
+                            "median_rel_err_grad": float(np.median(grel)),
+                            "rel_err_definition": "per system max|g32-g64| / max|g64| over its values",
+                            "bound": 1e-5},
                 "serving": served,
                 "wall_s_timed_region": t_wall}
         if world == 1:

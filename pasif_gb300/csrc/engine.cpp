@@ -419,7 +419,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     const size_t Bn = (size_t)B;
     PK_CUDA(ckpt.ensure(Bn * 2 * n * (size_t)(nck > 0 ? nck : 1) * rs), "cudaMalloc");
     PK_CUDA(buf.ensure(Bn * (size_t)n * (size_t)C * rs), "cudaMalloc");
-    PK_CUDA(scratch.ensure(Bn * 13 * (size_t)n * rs), "cudaMalloc");
+    PK_CUDA(scratch.ensure(Bn * 14 * (size_t)n * rs), "cudaMalloc");   // adj_run_generic's 14 vectors
     PK_CUDA(pbar.ensure(Bn * (size_t)(P > 0 ? P : 1) * sizeof(double)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     if (g_final) {

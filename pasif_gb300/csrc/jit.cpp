@@ -502,10 +502,12 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
                 }
             }
             o << "  }\n";
-            o << "  template <class V> __device__ __forceinline__ void add_sq_grad(V& LAM, const V& QN, R g) const {\n";
+            o << "  template <bool KAHAN, class V> __device__ __forceinline__ void add_sq_grad(V& LAM, V& CL, const V& QN,"
+                 " R g) const {\n";
             for (int k = 0; k < MM; ++k)
                 if (own[k] < 64 && ((key.sq_mask >> own[k]) & 1ull))
-                    o << "    LAM[" << k << "] = M<R>::fma(g, QN[" << k << "], LAM[" << k << "]);\n";
+                    o << "    if (KAHAN) kahan_add(LAM[" << k << "], CL[" << k << "], M<R>::mul(g, QN[" << k
+                      << "])); else LAM[" << k << "] = M<R>::fma(g, QN[" << k << "], LAM[" << k << "]);\n";
             o << "  }\n";
             o << "  template <class PV> __device__ __forceinline__ void store_pbar(const PV& PB, double* pbar, long long B,"
                  " int b) const {\n";

@@ -83,6 +83,15 @@ __device__ __forceinline__ R force_at(const Forcing<R>& f, long long ebase, unsi
 // Parameter-gradient accumulation: into FP64 (fma of the FP32 or FP64
 // factors promoted to double) or, for per-step partial sums, in the compute
 // precision.
+// s += inc with compensation c (the Kahan form of the state update).
+template <typename R>
+__device__ __forceinline__ void kahan_add(R& s, R& c, R inc) {
+    const R y = M<R>::sub(inc, c);
+    const R t = M<R>::add(s, y);
+    c = M<R>::sub(M<R>::sub(t, s), y);
+    s = t;
+}
+
 __device__ __forceinline__ void pacc_add(double& p, double x, double y) { p = __fma_rn(x, y, p); }
 __device__ __forceinline__ void pacc_add(double& p, float x, float y) { p = __fma_rn((double)x, (double)y, p); }
 __device__ __forceinline__ void pacc_add(float& p, float x, float y) { p = __fmaf_rn(x, y, p); }
@@ -541,9 +550,9 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
         if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
         else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
     }
-    RegVec<R, N> LAM, QN;
+    RegVec<R, N> LAM, QN, CL;   // CL: compensation of LAM (Kahan mode)
 #pragma unroll
-    for (int i = 0; i < N; ++i) LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0);
+    for (int i = 0; i < N; ++i) { LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0); CL[i] = R(0); }
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
     for (int k = a.nck - 1; k >= 0; --k) {
         const int start = k * a.C;
@@ -572,7 +581,10 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
             if (HSQ && a.g_sq && t >= a.sq_start) {
 #pragma unroll
                 for (int i = 0; i < N; ++i)
-                    if (i < 64 && ((sq_mask >> i) & 1ull)) LAM[i] = m::fma(gsq2h, QN[i], LAM[i]);
+                    if (i < 64 && ((sq_mask >> i) & 1ull)) {
+                        if (a.kahan) kahan_add(LAM[i], CL[i], m::mul(gsq2h, QN[i]));
+                        else LAM[i] = m::fma(gsq2h, QN[i], LAM[i]);
+                    }
             }
             const unsigned st = (unsigned)t;
             const R ua = force_at(a.frc, ebase, st, 0u, 0u);
@@ -585,8 +597,14 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
 #pragma unroll
             for (int i = 0; i < N; ++i) Y3[i] = m::fma(a.h2, K[i], QC[i]);
             sys.template rhs<true>(Y3, Y3, ub, K);
+            // QB sums the step's increment of LAM: onto LAM itself (plain), or
+            // from 0 and then added with compensation (Kahan mode)
 #pragma unroll
-            for (int i = 0; i < N; ++i) { Y4[i] = m::fma(a.h, K[i], QC[i]); KB[i] = m::mul(a.h6, LAM[i]); QB[i] = LAM[i]; }
+            for (int i = 0; i < N; ++i) {
+                Y4[i] = m::fma(a.h, K[i], QC[i]);
+                KB[i] = m::mul(a.h6, LAM[i]);
+                QB[i] = a.kahan ? R(0) : LAM[i];
+            }
             sys.vjp(Y4, KB, uc, YB, pacc);
 #pragma unroll
             for (int i = 0; i < N; ++i) {
@@ -610,7 +628,11 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
             }
             sys.vjp(QC, KB, ua, YB, pacc);
 #pragma unroll
-            for (int i = 0; i < N; ++i) { LAM[i] = m::add(QB[i], YB[i]); QN[i] = QC[i]; }
+            for (int i = 0; i < N; ++i) {
+                if (a.kahan) kahan_add(LAM[i], CL[i], m::add(QB[i], YB[i]));
+                else LAM[i] = m::add(QB[i], YB[i]);
+                QN[i] = QC[i];
+            }
             if (STEP_ACC) {
 #pragma unroll
                 for (int p = 0; p < P; ++p) { PB[p] = PB[p] + (double)pacc[p]; pacc[p] = R(0); }
@@ -641,7 +663,7 @@ __device__ void adj_run_generic(const Sys& sys, const AdjArgs<R>& a, int b) {
         K{base + 3LL * n * B, B}, Mi{base + 4LL * n * B, B}, Y2{base + 5LL * n * B, B},
         Y3{base + 6LL * n * B, B}, Y4{base + 7LL * n * B, B}, LAM{base + 8LL * n * B, B},
         QB{base + 9LL * n * B, B}, KB{base + 10LL * n * B, B}, YB{base + 11LL * n * B, B},
-        QN{base + 12LL * n * B, B};
+        QN{base + 12LL * n * B, B}, CL{base + 13LL * n * B, B};   // CL: LAM compensation (Kahan mode)
     GVec<double> PB{a.pbar + b, B};
     const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
     const int P = sys.g.P;
@@ -660,7 +682,7 @@ __device__ void adj_run_generic(const Sys& sys, const AdjArgs<R>& a, int b) {
         if (a.kahan) rk4_step<R, 0, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
         else rk4_step<R, 0, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
     }
-    for (int i = 0; i < n; ++i) LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0);
+    for (int i = 0; i < n; ++i) { LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0); CL[i] = R(0); }
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
     for (int k = a.nck - 1; k >= 0; --k) {
         const int start = k * a.C;
@@ -682,7 +704,16 @@ __device__ void adj_run_generic(const Sys& sys, const AdjArgs<R>& a, int b) {
             GVec<R> QC{a.buf + (long long)(t - start) * n * B + b, B};
             if (a.g_sq && t >= a.sq_start)
                 for (int i = 0; i < n; ++i)
-                    if (i < 64 && ((a.sq_mask >> i) & 1ull)) LAM[i] = m::fma(gsq2h, QN[i], LAM[i]);
+                    if (i < 64 && ((a.sq_mask >> i) & 1ull)) {
+                        if (a.kahan) {
+                            R l = LAM[i], c = CL[i];
+                            kahan_add(l, c, m::mul(gsq2h, QN[i]));
+                            LAM[i] = l;
+                            CL[i] = c;
+                        } else {
+                            LAM[i] = m::fma(gsq2h, QN[i], LAM[i]);
+                        }
+                    }
             const unsigned st = (unsigned)t;
             const R ua = force_at(a.frc, ebase, st, 0u, 0u);
             const R ub = force_at(a.frc, ebase, st, 0u, 1u);
@@ -693,8 +724,8 @@ __device__ void adj_run_generic(const Sys& sys, const AdjArgs<R>& a, int b) {
             for (int i = 0; i < n; ++i) Y3[i] = m::fma(a.h2, K[i], QC[i]);
             sys.template rhs<true>(Y3, Y3, ub, K);
             for (int i = 0; i < n; ++i) Y4[i] = m::fma(a.h, K[i], QC[i]);
-            // kb4 = sb; qb = lam
-            for (int i = 0; i < n; ++i) { KB[i] = m::mul(a.h6, LAM[i]); QB[i] = LAM[i]; }
+            // kb4 = sb; qb = lam (plain) or the increment from 0 (Kahan mode)
+            for (int i = 0; i < n; ++i) { KB[i] = m::mul(a.h6, LAM[i]); QB[i] = a.kahan ? R(0) : LAM[i]; }
             sys.vjp(Y4, KB, uc, YB, PB);
             for (int i = 0; i < n; ++i) {
                 const R sb = m::mul(a.h6, LAM[i]);
@@ -714,7 +745,17 @@ __device__ void adj_run_generic(const Sys& sys, const AdjArgs<R>& a, int b) {
                 KB[i] = m::fma(a.h2, YB[i], sb);
             }
             sys.vjp(QC, KB, ua, YB, PB);
-            for (int i = 0; i < n; ++i) { LAM[i] = m::add(QB[i], YB[i]); QN[i] = QC[i]; }
+            for (int i = 0; i < n; ++i) {
+                if (a.kahan) {
+                    R l = LAM[i], c = CL[i];
+                    kahan_add(l, c, m::add(QB[i], YB[i]));
+                    LAM[i] = l;
+                    CL[i] = c;
+                } else {
+                    LAM[i] = m::add(QB[i], YB[i]);
+                }
+                QN[i] = QC[i];
+            }
         }
     }
     for (int i = 0; i < n; ++i) a.dx0[i * B + b] = LAM[i];
@@ -1036,12 +1077,14 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
         const R uc = force_at(a.frc, ebase, st, 1u, 0u);
         ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
     }
-    V LAM, QN;
+    V LAM, QN, CL;   // CL: compensation of LAM (Kahan mode)
     if (a.g_final) sl.load_vec(LAM, a.g_final, B, b);
     else {
 #pragma unroll
         for (int i = 0; i < MM; ++i) LAM[i] = R(0);
     }
+#pragma unroll
+    for (int i = 0; i < MM; ++i) CL[i] = R(0);
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
     for (int k = a.nck - 1; k >= 0; --k) {
         const int start = k * a.C;
@@ -1065,7 +1108,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             V QC, Y2, Y3, Y4, QB, KB, YB;
             // the chunk states were written by this thread (own components) before the barriers above
             sl.load_vec(QC, a.buf + (long long)(t - start) * N * B, B, b);
-            if (HSQ && a.g_sq && t >= a.sq_start) sl.add_sq_grad(LAM, QN, gsq2h);
+            if (HSQ && a.g_sq && t >= a.sq_start) sl.template add_sq_grad<KAHAN>(LAM, CL, QN, gsq2h);
             const unsigned st = (unsigned)t;
             const R ua = force_at(a.frc, ebase, st, 0u, 0u);
             const R ub = force_at(a.frc, ebase, st, 0u, 1u);
@@ -1092,7 +1135,11 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                     for (int i = 0; i < MM; ++i) Y3[i] = Yc[i];
                 } else {
 #pragma unroll
-                    for (int i = 0; i < MM; ++i) { Y4[i] = Yc[i]; KB[i] = m::mul(a.h6, LAM[i]); QB[i] = LAM[i]; }
+                    for (int i = 0; i < MM; ++i) {
+                        Y4[i] = Yc[i];
+                        KB[i] = m::mul(a.h6, LAM[i]);
+                        QB[i] = KAHAN ? R(0) : LAM[i];   // the step's increment (Kahan) or LAM + it
+                    }
                     sl.publish(KB, k0);
                 }
                 sl.publish(Yc, rq + (st + 1) * NP * 32);
@@ -1127,7 +1174,11 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                 pk_block_sync();
             }
 #pragma unroll
-            for (int i = 0; i < MM; ++i) { LAM[i] = m::add(QB[i], YB[i]); QN[i] = QC[i]; }
+            for (int i = 0; i < MM; ++i) {
+                if (KAHAN) kahan_add(LAM[i], CL[i], m::add(QB[i], YB[i]));
+                else LAM[i] = m::add(QB[i], YB[i]);
+                QN[i] = QC[i];
+            }
             if constexpr (STEP_ACC) {
                 if (valid) sl.add_pbar(pst, a.pbar, B, b);
 #pragma unroll

@@ -2,8 +2,10 @@
 // device-resident batches, kernel selection and launch).
 #include "engine.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "generic_kernels.h"
 
@@ -463,22 +465,41 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
                      get_adj_kernel(pat, lit, f, plan->precision == kFP32Kahan, g_sq ? sm : 0ull, slices, &jk, &jerr);
     if (!jit && !plan->generic_only) last_jit_error = jerr;
     const dim3 grid((unsigned)(jit ? (B + jk.per_block - 1) / jk.per_block : (B + 127) / 128));
+    if (jit && plan->precision == kFP32Kahan) PK_CUDA(lamc.ensure(Bn * (size_t)n * rs), "cudaMalloc");
+    // Specialised kernels: one launch for short horizons, else forward segments and
+    // backward chunk groups of about kAdjLaunchSteps steps each, so that a launch
+    // lasts milliseconds and work on other streams (serving chunks) is not held
+    // behind a whole adjoint.
+    auto launch_jit = [&](auto& a) -> cudaError_t {
+        void* args[] = {&a};
+        a.lamc = lamc.as<typename std::remove_pointer<decltype(a.dx0)>::type>();
+        const int per = std::max(1, kAdjLaunchSteps / C);   // checkpoint intervals per launch
+        if (nck <= 2 * per) {
+            a.phase = 0;
+            return cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
+        }
+        for (int t0 = 0; t0 < nsteps; t0 += per * C) {
+            a.phase = 1;
+            a.t_begin = t0;
+            a.t_end = std::min(nsteps, t0 + per * C);
+            cudaError_t le = cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
+            if (le != cudaSuccess) return le;
+        }
+        for (int khi = nck - 1; khi >= 0; khi -= per) {
+            a.phase = 2;
+            a.k_hi = khi;
+            a.k_lo = std::max(0, khi - per + 1);
+            cudaError_t le = cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
+            if (le != cudaSuccess) return le;
+        }
+        return cudaSuccess;
+    };
     if (f) {
         PK_FILL_ADJ(float)
-        if (jit) {
-            void* args[] = {&a};
-            e = cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
-        } else {
-            e = pk::launch_gen_adj(a, st);
-        }
+        e = jit ? launch_jit(a) : pk::launch_gen_adj(a, st);
     } else {
         PK_FILL_ADJ(double)
-        if (jit) {
-            void* args[] = {&a};
-            e = cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
-        } else {
-            e = pk::launch_gen_adj(a, st);
-        }
+        e = jit ? launch_jit(a) : pk::launch_gen_adj(a, st);
     }
 #undef PK_FILL_ADJ
     last_adj_kind = jit ? kSpecialised : kGeneric;

@@ -17,6 +17,9 @@ enum Precision { kFP64 = 0, kFP32 = 1, kFP32Kahan = 2 };
 enum Memory { kHost = 0, kDevice = 1 };
 enum KernelKind { kNone = 0, kGeneric = 1, kSpecialised = 2 };
 
+// Steps per launch of a split exact adjoint (forward segments, backward chunk groups).
+constexpr int kAdjLaunchSteps = 2048;
+
 // Growable device allocation.
 struct DevBuf {
     void* p = nullptr;
@@ -86,7 +89,7 @@ struct Batch {
     std::shared_ptr<Plan> plan;
     int B = 0;
     DevBuf vals, x0, state, exc, out_max, out_sq, scratch, stage, traj;
-    DevBuf ckpt, buf, pbar, dx0, gfin, gsq, adj_stage;
+    DevBuf ckpt, buf, pbar, dx0, gfin, gsq, adj_stage, lamc;
     Literals lit;
     int n_max = 0;
     bool has_sq = false;

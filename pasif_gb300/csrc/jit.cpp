@@ -513,6 +513,10 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
                  " int b) const {\n";
             for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = PB[" << kv.second << "];\n";
             o << "  }\n";
+            o << "  template <class PV> __device__ __forceinline__ void load_pbar(PV& PB, const double* pbar, long long B,"
+                 " int b) const {\n";
+            for (auto& kv : pslot) o << "    PB[" << kv.second << "] = pbar[" << kv.first << "LL * B + b];\n";
+            o << "  }\n";
             o << "  __device__ __forceinline__ void zero_pbar(double* pbar, long long B, int b) const {\n";
             for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = 0.0;\n";
             o << "  }\n";

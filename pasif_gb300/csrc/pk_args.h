@@ -101,6 +101,15 @@ struct AdjArgs {
     int kahan;
     int sq_start;
     unsigned long long sq_mask;
+    // Launch split (pattern-specialised kernels): phase 0 = the whole adjoint in
+    // one launch; 1 = forward pass over steps [t_begin, t_end) (multiples of C
+    // except t_end = nsteps), state carried in the checkpoints; 2 = backward
+    // over chunks k_hi down to k_lo, the adjoint state carried in dx0 (and its
+    // compensation in lamc).  Short launches let other streams' work in.
+    int phase;
+    int t_begin, t_end;
+    int k_lo, k_hi;
+    R* lamc;                    // [n][B] (Kahan mode)
 };
 
 // __GpuDriver::_getGradient semantics (see the oracle for the quirk list).

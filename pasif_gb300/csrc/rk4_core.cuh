@@ -530,31 +530,54 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
     GVec<double> PB{a.pbar + b, B};
     const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
     RegVec<R, N> Q, Cm, S, K, Mi;
-    for (int p = 0; p < P; ++p) PB[p] = 0.0;
     if (STEP_ACC) {
 #pragma unroll
         for (int p = 0; p < P; ++p) pacc[p] = R(0);
     }
+    if (a.phase != 2) {   // forward pass with checkpoints
+        const int t0 = a.phase == 1 ? a.t_begin : 0, t1 = a.phase == 1 ? a.t_end : a.nsteps;
+        if (t0 == 0) {
+            for (int p = 0; p < P; ++p) PB[p] = 0.0;
 #pragma unroll
-    for (int i = 0; i < N; ++i) { Q[i] = a.x0[i * B + b]; Cm[i] = R(0); }
-    for (int t = 0; t < a.nsteps; ++t) {
-        if (t % a.C == 0) {
-            R* ck = a.ckpt + (long long)(t / a.C) * 2 * N * B + b;
+            for (int i = 0; i < N; ++i) { Q[i] = a.x0[i * B + b]; Cm[i] = R(0); }
+        } else {
+            const R* ck = a.ckpt + (long long)(t0 / a.C) * 2 * N * B + b;
 #pragma unroll
-            for (int i = 0; i < N; ++i) { ck[i * B] = Q[i]; ck[(N + i) * B] = Cm[i]; }
+            for (int i = 0; i < N; ++i) { Q[i] = ck[i * B]; Cm[i] = ck[(N + i) * B]; }
         }
-        const unsigned st = (unsigned)t;
-        const R ua = force_at(a.frc, ebase, st, 0u, 0u);
-        const R ub = force_at(a.frc, ebase, st, 0u, 1u);
-        const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-        if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
-        else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+        for (int t = t0; t < t1; ++t) {
+            if (t % a.C == 0) {
+                R* ck = a.ckpt + (long long)(t / a.C) * 2 * N * B + b;
+#pragma unroll
+                for (int i = 0; i < N; ++i) { ck[i * B] = Q[i]; ck[(N + i) * B] = Cm[i]; }
+            }
+            const unsigned st = (unsigned)t;
+            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+            else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+        }
+        if (a.phase == 1) {   // the next segment starts from this checkpoint
+            if (t1 < a.nsteps && t1 % a.C == 0) {
+                R* ck = a.ckpt + (long long)(t1 / a.C) * 2 * N * B + b;
+#pragma unroll
+                for (int i = 0; i < N; ++i) { ck[i * B] = Q[i]; ck[(N + i) * B] = Cm[i]; }
+            }
+            return;
+        }
     }
     RegVec<R, N> LAM, QN, CL;   // CL: compensation of LAM (Kahan mode)
+    const int khi = a.phase == 2 ? a.k_hi : a.nck - 1, klo = a.phase == 2 ? a.k_lo : 0;
+    if (khi == a.nck - 1) {
 #pragma unroll
-    for (int i = 0; i < N; ++i) { LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0); CL[i] = R(0); }
+        for (int i = 0; i < N; ++i) { LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0); CL[i] = R(0); }
+    } else {   // carried from the previous backward launch
+#pragma unroll
+        for (int i = 0; i < N; ++i) { LAM[i] = a.dx0[i * B + b]; CL[i] = a.kahan ? a.lamc[i * B + b] : R(0); }
+    }
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
-    for (int k = a.nck - 1; k >= 0; --k) {
+    for (int k = khi; k >= klo; --k) {
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
         const R* ck = a.ckpt + (long long)k * 2 * N * B + b;
@@ -640,7 +663,10 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
         }
     }
 #pragma unroll
-    for (int i = 0; i < N; ++i) a.dx0[i * B + b] = LAM[i];
+    for (int i = 0; i < N; ++i) {
+        a.dx0[i * B + b] = LAM[i];
+        if (a.phase == 2 && a.kahan) a.lamc[i * B + b] = CL[i];
+    }
 }
 
 // Exact discrete adjoint of the RK4 map for one instance (generic storage):
@@ -1056,37 +1082,65 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     for (int p = 0; p < (STEP_ACC ? 1 : PO); ++p) PB[p] = 0.0;
 #pragma unroll
     for (int p = 0; p < (STEP_ACC ? PO : 1); ++p) pst[p] = R(0);
-    if constexpr (STEP_ACC) {
-        if (valid) sl.zero_pbar(a.pbar, B, b);
-    }
     V Q, Cm, S, K, Mi;
-    sl.load_vec(Q, a.x0, B, b);
+    if (a.phase != 2) {   // forward pass with checkpoints (phase 1: steps [t_begin, t_end))
+        const int t0 = a.phase == 1 ? a.t_begin : 0, t1 = a.phase == 1 ? a.t_end : a.nsteps;
+        if (t0 == 0) {
+            if constexpr (STEP_ACC) {
+                if (valid) sl.zero_pbar(a.pbar, B, b);
+            }
+            sl.load_vec(Q, a.x0, B, b);
 #pragma unroll
-    for (int i = 0; i < MM; ++i) Cm[i] = R(0);
-    sl.publish(Q, rq);
-    pk_block_sync();
-    for (int t = 0; t < a.nsteps; ++t) {
-        if (t % a.C == 0 && valid) {
-            R* ck = a.ckpt + (long long)(t / a.C) * 2 * N * B;
-            sl.store_vec(Q, ck, B, b);
-            sl.store_vec(Cm, ck + (long long)N * B, B, b);
+            for (int i = 0; i < MM; ++i) Cm[i] = R(0);
+        } else {
+            const R* ck = a.ckpt + (long long)(t0 / a.C) * 2 * N * B;
+            sl.load_vec(Q, ck, B, b);
+            sl.load_vec(Cm, ck + (long long)N * B, B, b);
         }
-        const unsigned st = (unsigned)t;
-        const R ua = force_at(a.frc, ebase, st, 0u, 0u);
-        const R ub = force_at(a.frc, ebase, st, 0u, 1u);
-        const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-        ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
+        sl.publish(Q, rq);
+        pk_block_sync();
+        for (int t = t0; t < t1; ++t) {
+            if (t % a.C == 0 && valid) {
+                R* ck = a.ckpt + (long long)(t / a.C) * 2 * N * B;
+                sl.store_vec(Q, ck, B, b);
+                sl.store_vec(Cm, ck + (long long)N * B, B, b);
+            }
+            const unsigned st = (unsigned)t;
+            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
+        }
+        if (a.phase == 1) {   // the next segment starts from this checkpoint
+            if (valid && t1 < a.nsteps && t1 % a.C == 0) {
+                R* ck = a.ckpt + (long long)(t1 / a.C) * 2 * N * B;
+                sl.store_vec(Q, ck, B, b);
+                sl.store_vec(Cm, ck + (long long)N * B, B, b);
+            }
+            return;
+        }
     }
     V LAM, QN, CL;   // CL: compensation of LAM (Kahan mode)
-    if (a.g_final) sl.load_vec(LAM, a.g_final, B, b);
-    else {
+    const int khi = a.phase == 2 ? a.k_hi : a.nck - 1, klo = a.phase == 2 ? a.k_lo : 0;
+    if (khi == a.nck - 1) {
+        if (a.g_final) sl.load_vec(LAM, a.g_final, B, b);
+        else {
 #pragma unroll
-        for (int i = 0; i < MM; ++i) LAM[i] = R(0);
+            for (int i = 0; i < MM; ++i) LAM[i] = R(0);
+        }
+#pragma unroll
+        for (int i = 0; i < MM; ++i) CL[i] = R(0);
+    } else {   // carried from the previous backward launch
+        sl.load_vec(LAM, a.dx0, B, b);
+        if (KAHAN) sl.load_vec(CL, a.lamc, B, b);
+        else {
+#pragma unroll
+            for (int i = 0; i < MM; ++i) CL[i] = R(0);
+        }
+        if constexpr (!STEP_ACC) sl.load_pbar(PB, a.pbar, B, b);
     }
-#pragma unroll
-    for (int i = 0; i < MM; ++i) CL[i] = R(0);
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
-    for (int k = a.nck - 1; k >= 0; --k) {
+    for (int k = khi; k >= klo; --k) {
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
         const R* ck = a.ckpt + (long long)k * 2 * N * B;
@@ -1189,6 +1243,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     }
     if (!valid) return;
     sl.store_vec(LAM, a.dx0, B, b);
+    if (KAHAN && a.phase == 2) sl.store_vec(CL, a.lamc, B, b);
     if constexpr (!STEP_ACC) sl.store_pbar(PB, a.pbar, B, b);
 }
 

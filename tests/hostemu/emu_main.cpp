@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <barrier>
 #include <thread>
 #include <vector>
@@ -273,7 +274,28 @@ int main(int argc, char** argv) {
     a.nck = nck;
     a.kahan = kahan;
     a.sq_start = sq_start;
-    for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_adj(a); });
+    std::vector<R> lamc((size_t)B * n, R(0));
+    a.lamc = lamc.data();
+    // EMU_ADJ_SPLIT=k: the launch split of Batch::adjoint with k checkpoint
+    // intervals per launch (forward segments, then backward chunk groups)
+    const char* split = std::getenv("EMU_ADJ_SPLIT");
+    const int per = split ? std::atoi(split) : 0;
+    if (per <= 0 || nck <= 2 * per) {
+        for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_adj(a); });
+    } else {
+        for (int t0 = 0; t0 < nsteps; t0 += per * C) {
+            a.phase = 1;
+            a.t_begin = t0;
+            a.t_end = std::min(nsteps, t0 + per * C);
+            for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_adj(a); });
+        }
+        for (int khi = nck - 1; khi >= 0; khi -= per) {
+            a.phase = 2;
+            a.k_hi = khi;
+            a.k_lo = std::max(0, khi - per + 1);
+            for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_adj(a); });
+        }
+    }
     std::snprintf(path, sizeof path, "%s/pbar.bin", dir);
     FILE* f = std::fopen(path, "wb");
     std::fwrite(pbar.data(), sizeof(double), pbar.size(), f);

@@ -79,12 +79,16 @@ def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps,
     np.testing.assert_array_equal(got, ref)
 
 
-def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, sq_start, h=0.03):
+def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, sq_start, h=0.03, split=0):
+    """split > 0: run it as the split launches of Batch::adjoint with `split`
+    checkpoint intervals per launch."""
     mask = sum(1 << c for c in sq)
     src = Plan(pat, prec, slicing=slicing).jit_report_adjoint(vals, sq_mask=mask)
     src = src.split("// ---- source ----\n", 1)[1]
     assert ("warp-sliced" in src) == bool(slicing)
     exe, env = build_emulator(d, src, "EMU_ADJ")
+    if split:
+        env["EMU_ADJ_SPLIT"] = str(split)
     dt = np.float64 if prec == "fp64" else np.float32
     B = len(vals)
     np.ascontiguousarray(vals.T, dt).tofile(os.path.join(d, "vals.bin"))
@@ -246,3 +250,20 @@ def test_generated_warp_sliced_banded32(tmp_path, prec):
     ref, _, _ = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
                                 prec)
     np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
+@pytest.mark.parametrize("slicing", [False, True])
+@pytest.mark.parametrize("split", [1, 2])
+def test_generated_adjoint_split_launches(tmp_path, prec, slicing, split):
+    """The adjoint split into short launches (forward segments carrying the
+    state in the checkpoints, backward chunk groups carrying the adjoint state
+    and its compensation) equals the single launch bit for bit."""
+    pat, vals, x0, exc, x, im, gf, gs, N, sq = _adjoint_case(2)
+    out = []
+    for sp in (0, split):
+        d = os.path.join(str(tmp_path), str(sp))
+        os.makedirs(d)
+        out.append(run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, N // 3, split=sp))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])

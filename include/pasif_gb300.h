@@ -200,6 +200,10 @@ int pasif_batch_destroy(pasif_batch* b);
 /* New instance count for the next pasif_batch_set; device buffers are kept
  * and grown only when too small (a batch reused across requests). */
 int pasif_batch_resize(pasif_batch* b, int n_sys);
+/* Grow the batch's device buffers to what a forward or exact adjoint of
+ * n_sys instances over nsteps steps needs, so later calls up to that size
+ * allocate nothing (cudaMalloc/cudaFree synchronise the device). */
+int pasif_batch_reserve(pasif_batch* b, int n_sys, int nsteps);
 /* values[n_sys][P], x0[n_sys][n], exc_index[n_sys]. */
 int pasif_batch_set(pasif_batch* b, const double* values, const double* x0, const int* exc_index,
                     int memory, void* stream);

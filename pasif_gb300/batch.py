@@ -135,6 +135,11 @@ class Batch:
         self._h = 0.0
         self.set(values, x0, exc_index, stream)
 
+    def reserve(self, n_sys: int, nsteps: int):
+        """Size the device buffers for forward / adjoint solves of up to n_sys
+        instances and nsteps steps (later calls then allocate nothing)."""
+        N.check(N.lib.pasif_batch_reserve(self.handle, int(n_sys), int(nsteps)))
+
     def set(self, values, x0, exc_index, stream=None):
         """New inputs; a different instance count resizes the batch (its
         device buffers are kept, and grown only when too small)."""

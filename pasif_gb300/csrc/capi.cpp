@@ -352,6 +352,14 @@ int pasif_batch_resize(pasif_batch* b, int n_sys) {
     return done(b->b->resize(n_sys, &err), err);
 }
 
+int pasif_batch_reserve(pasif_batch* b, int n_sys, int nsteps) {
+    if (!b || !b->b) return fail(PASIF_ERR_INVALID, "null batch");
+    return guard([&] {
+        std::string err;
+        return done(b->b->reserve(n_sys, nsteps, &err), err);
+    });
+}
+
 int pasif_batch_create(pasif_batch** out, pasif_plan* plan, int n_sys) {
     return guard([&] {
         if (!out || !plan) return fail(PASIF_ERR_INVALID, "null handle");

@@ -148,11 +148,38 @@ int signals_update(Signals& s, const double* x, int n_exc, int len, int memory, 
     return 0;
 }
 
+int Batch::reserve(int n_sys, int nsteps, std::string* err) {
+    if (n_sys < 0 || nsteps < 0) { *err = "negative reservation"; return 1; }
+    const Pattern& pat = plan->pat;
+    const size_t n = (size_t)pat.n, P = (size_t)(pat.P() > 0 ? pat.P() : 1), rs = rsize();
+    const size_t Bn = (size_t)(n_sys > 0 ? n_sys : 1), wide = std::max(P, n);
+    const size_t C = nsteps > 0 ? (size_t)std::ceil(std::sqrt((double)nsteps)) : 1;
+    const size_t nck = nsteps > 0 ? ((size_t)nsteps + C - 1) / C : 1;
+    PK_CUDA(vals.ensure(Bn * P * rs), "cudaMalloc");
+    PK_CUDA(x0.ensure(Bn * n * rs), "cudaMalloc");
+    PK_CUDA(stage.ensure(Bn * wide * sizeof(double)), "cudaMalloc");
+    PK_CUDA(exc.ensure(Bn * sizeof(int)), "cudaMalloc");
+    PK_CUDA(state.ensure(Bn * n * rs), "cudaMalloc");
+    PK_CUDA(out_max.ensure(Bn * n * rs), "cudaMalloc");
+    PK_CUDA(out_sq.ensure(Bn * rs), "cudaMalloc");
+    PK_CUDA(ckpt.ensure(Bn * 2 * n * nck * rs), "cudaMalloc");
+    PK_CUDA(buf.ensure(Bn * n * C * rs), "cudaMalloc");
+    PK_CUDA(pbar.ensure(Bn * P * sizeof(double)), "cudaMalloc");
+    PK_CUDA(dx0.ensure(Bn * n * rs), "cudaMalloc");
+    PK_CUDA(gfin.ensure(Bn * n * rs), "cudaMalloc");
+    PK_CUDA(gsq.ensure(Bn * rs), "cudaMalloc");
+    PK_CUDA(lamc.ensure(Bn * n * rs), "cudaMalloc");
+    PK_CUDA(adj_stage.ensure(Bn * wide * sizeof(double)), "cudaMalloc");
+    inputs_set = false;   // grown buffers are fresh allocations
+    return 0;
+}
+
 int Batch::resize(int n_sys, std::string* err) {
     if (n_sys < 0) { *err = "negative number of systems"; return 1; }
     B = n_sys;
     max_exc_ = -1;
     last_kind = last_adj_kind = kNone;
+    inputs_set = false;
     return 0;
 }
 
@@ -247,6 +274,7 @@ int Batch::set(const double* values, const double* x0h, const int* exc_index, in
         }
     }
     PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    inputs_set = true;
     return 0;
 }
 
@@ -299,6 +327,7 @@ int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Re
     const bool f = f32();
     if (sig.f32 != f) { *err = "signal table precision differs from the plan's"; return 1; }
     if (step0 < 0 || nsteps < 0) { *err = "negative step index or step count"; return 1; }
+    if (B > 0 && !inputs_set) { *err = "batch inputs not set (set them after creating, resizing or reserving)"; return 5; }
     if (max_exc_ >= sig.n_exc) { *err = "excitation index beyond the signal table"; return 1; }
     if (!(h > 0.0) || !std::isfinite(h)) { *err = "time step must be positive and finite"; return 1; }
     unsigned long long mm = 0, sm = 0;
@@ -410,6 +439,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     const bool f = f32();
     if (sig.f32 != f) { *err = "signal table precision differs from the plan's"; return 1; }
     if (nsteps < 0) { *err = "negative step count"; return 1; }
+    if (B > 0 && !inputs_set) { *err = "batch inputs not set (set them after creating, resizing or reserving)"; return 5; }
     if (max_exc_ >= sig.n_exc) { *err = "excitation index beyond the signal table"; return 1; }
     if (!(h > 0.0) || !std::isfinite(h)) { *err = "time step must be positive and finite"; return 1; }
     unsigned long long sm = 0;
@@ -421,7 +451,6 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     const size_t Bn = (size_t)B;
     PK_CUDA(ckpt.ensure(Bn * 2 * n * (size_t)(nck > 0 ? nck : 1) * rs), "cudaMalloc");
     PK_CUDA(buf.ensure(Bn * (size_t)n * (size_t)C * rs), "cudaMalloc");
-    PK_CUDA(scratch.ensure(Bn * 14 * (size_t)n * rs), "cudaMalloc");   // adj_run_generic's 14 vectors
     PK_CUDA(pbar.ensure(Bn * (size_t)(P > 0 ? P : 1) * sizeof(double)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     if (g_final) {
@@ -466,15 +495,18 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     if (!jit && !plan->generic_only) last_jit_error = jerr;
     const dim3 grid((unsigned)(jit ? (B + jk.per_block - 1) / jk.per_block : (B + 127) / 128));
     if (jit && plan->precision == kFP32Kahan) PK_CUDA(lamc.ensure(Bn * (size_t)n * rs), "cudaMalloc");
-    // Specialised kernels: one launch for short horizons, else forward segments and
-    // backward chunk groups of about kAdjLaunchSteps steps each, so that a launch
-    // lasts milliseconds and work on other streams (serving chunks) is not held
-    // behind a whole adjoint.
+    // Specialised kernels over many blocks: forward segments and backward chunk
+    // groups of about kAdjLaunchSteps·16/n steps each, so that a launch lasts
+    // milliseconds and work on other streams (serving chunks, small adjoints) is
+    // not held behind a whole adjoint that fills the SMs.  Small grids (a few
+    // SMs) and short horizons run as one launch: split, each of their launches
+    // would wait again for SMs held by others.
     auto launch_jit = [&](auto& a) -> cudaError_t {
         void* args[] = {&a};
         a.lamc = lamc.as<typename std::remove_pointer<decltype(a.dx0)>::type>();
-        const int per = std::max(1, kAdjLaunchSteps / C);   // checkpoint intervals per launch
-        if (nck <= 2 * per) {
+        const int steps = std::max(1, kAdjLaunchSteps * 16 / std::max(16, n));
+        const int per = std::max(1, steps / C);   // checkpoint intervals per launch
+        if (nck <= 2 * per || grid.x < 32) {
             a.phase = 0;
             return cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
         }
@@ -494,6 +526,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
         }
         return cudaSuccess;
     };
+    if (!jit) PK_CUDA(scratch.ensure(Bn * 14 * (size_t)n * rs), "cudaMalloc");   // adj_run_generic's 14 vectors
     if (f) {
         PK_FILL_ADJ(float)
         e = jit ? launch_jit(a) : pk::launch_gen_adj(a, st);

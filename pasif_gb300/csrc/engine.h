@@ -93,6 +93,7 @@ struct Batch {
     Literals lit;
     int n_max = 0;
     bool has_sq = false;
+    bool inputs_set = false;      // values / x0 / exc_index uploaded for the current B
     int max_exc_ = -1;
     double last_h = 0.0;          // time step of the last forward (scales sum q^2)
     int last_kind = kNone;
@@ -106,6 +107,11 @@ struct Batch {
     // New instance count; the device buffers are kept and grown by the next
     // set / solve when needed (a batch reused for requests of any size).
     int resize(int n_sys, std::string* err);
+    // Grow every device buffer to what a forward or an exact adjoint of n_sys
+    // instances over nsteps steps uses, so that later calls up to that size
+    // allocate nothing (no implicit device synchronisation).  A grown buffer
+    // does not keep its contents: the inputs must be set again.
+    int reserve(int n_sys, int nsteps, std::string* err);
     // values[B][P], x0[B][n] (double), exc_index[B]; host or device pointers.
     int set(const double* values, const double* x0h, const int* exc_index, int memory, cudaStream_t st,
             std::string* err);

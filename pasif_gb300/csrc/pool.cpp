@@ -94,6 +94,11 @@ int Pool::create(const Pattern& pat, int precision, int window, const double* im
     PL_CUDA(p->mstart_.ensure(C * sizeof(int)), "cudaMalloc");
     PL_CUDA(p->sstart_.ensure(C * sizeof(int)), "cudaMalloc");
     PL_CUDA(p->arena_.ensure((size_t)arena_samples * rs), "cudaMalloc");
+    // admission / harvest staging for a full pool and a table of up to 8M samples,
+    // so that serving does not allocate (an allocation synchronises the device)
+    PL_CUDA(p->scratch_.ensure(C * (sizeof(double) * (P + 3 * (size_t)n) + 64) +
+                               sizeof(double) * (size_t)std::min<long long>(arena_samples, 1LL << 23)),
+            "cudaMalloc");
     if (window > 0) {   // weights on the device for the steps outside whole intervals
         rc = upload_weights(im, window, f32, p->im_dev_, err);
         if (rc) return rc;

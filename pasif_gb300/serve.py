@@ -23,14 +23,15 @@ from . import synth
 
 
 def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, capacity=16384,
-        arena_samples=1 << 25, adjoint_budget=32 << 30, adjoint_workers=16, check=6, log=None) -> dict:
+        arena_samples=1 << 25, adjoint_budget=32 << 30, adjoint_workers=3, check=6, log=None) -> dict:
     dofs = tuple(dofs or synth.SERVED_DOFS)
     specs = S.served_specs(dofs)
     stream = synth.served_stream(rate, duration, seed, dofs=dofs)
     t = time.perf_counter()
     reqs = [(sr.arrival, S.make_request(sr, specs[sr.dof])) for sr in stream]
     t_gen = time.perf_counter() - t
-    srv = S.Server(specs, precision, capacity, arena_samples, adjoint_budget, adjoint_workers)
+    srv = S.Server(specs, precision, capacity, arena_samples, adjoint_budget, adjoint_workers,
+                   reserve=(4096, 200_000, 4 * 200_003))
     t = time.perf_counter()
     srv.warm()
     t_warm = time.perf_counter() - t
@@ -58,6 +59,12 @@ def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, cap
         "requests_per_s": len(ok) / out["wall_s"],
         "precision": precision, "chunk_launches": {str(k): v for k, v in sorted(chunks.items())},
         "kernels_ready_s": round(t_warm, 1),
+        "errors": sorted({x.error for x in res.values() if x.error})[:5],
+        "by_dof": {str(d): {kind: {"n": len(v), "p50_ms": round(S.percentile(v, 50), 1),
+                                   "p99_ms": round(S.percentile(v, 99), 1)}
+                            for kind in ("forward", "adjoint")
+                            for v in [[x.latency * 1e3 for x in ok if x.kind == kind and by_id[x.rid][0].dof == d]]}
+                   for d in dofs},
     }
     if check:
         summary.update(_check(specs, reqs, res, precision, check, seed))

@@ -187,14 +187,22 @@ class Server:
     """Continuous-batching server over one GPU.
 
     specs: class key -> ClassSpec.  Pools (one per class) are made on first
-    use or by warm().  pool_factory(spec) and adjoint_runner(spec, request,
-    stream) can be replaced (the host-only tests drive the scheduler with
-    fakes); the defaults run the CUDA kernels."""
+    use or by warm().  Adjoint requests queue per class and each class has
+    `adjoint_workers` workers, so cheap classes are not held behind long
+    adjoints of large systems (head-of-line blocking); the memory budget is
+    shared.  pool_factory(spec) and adjoint_runner(spec, request, stream) can
+    be replaced (the host-only tests drive the scheduler with fakes); the
+    defaults run the CUDA kernels."""
 
     def __init__(self, specs: dict, precision: str = "fp32_kahan", capacity: int = 8192,
                  arena_samples: int = 1 << 24, adjoint_budget: int = 8 << 30, adjoint_workers: int = 2,
-                 pool_factory=None, adjoint_runner=None, stream_factory=None, clock=time.perf_counter):
+                 pool_factory=None, adjoint_runner=None, stream_factory=None, clock=time.perf_counter,
+                 reserve=None):
+        """reserve = (max systems, max steps, max signal samples) of an adjoint
+        request: each worker sizes its batch and signal table for it on its
+        first request, so later ones allocate nothing."""
         self.specs = dict(specs)
+        self.reserve = reserve
         self.precision = precision
         self.capacity = int(capacity)
         self.arena_samples = int(arena_samples)
@@ -203,10 +211,16 @@ class Server:
         self._pool_factory = pool_factory or self._make_pool
         self._adjoint_runner = adjoint_runner or self._run_adjoint
         self._stream_factory = stream_factory or _torch_stream
+        # adjoint stream priority per class: the cheaper a system-step, the
+        # higher; their blocks then take SMs ahead of queued blocks of long
+        # large-system adjoints (the pools' streams have the highest priority)
+        cost = sorted(self.specs, key=lambda k: self.specs[k].pattern.flops_per_step())
+        self._prio = {k: -max(0, 4 - (4 * i) // max(1, len(cost) - 1)) if len(cost) > 1 else 0
+                      for i, k in enumerate(cost)}
         self._cv = threading.Condition()
         self._pools = {}
         self._fwd_q = collections.defaultdict(collections.deque)
-        self._adj_q = collections.deque()
+        self._adj_q = collections.defaultdict(collections.deque)   # per class
         self._adj_used = 0
         self._results = {}
         self._outstanding = 0
@@ -252,10 +266,11 @@ class Server:
 
     def start(self) -> None:
         self.t0 = self.clock()
-        for i in range(self._n_adj_workers):
-            t = threading.Thread(target=self._adj_loop, daemon=True, name=f"adjoint-{i}")
-            self._threads.append(t)
-            t.start()
+        for key in self.specs:
+            for i in range(self._n_adj_workers):
+                t = threading.Thread(target=self._adj_loop, args=(key,), daemon=True, name=f"adjoint-{key}-{i}")
+                self._threads.append(t)
+                t.start()
 
     def stop(self) -> None:
         with self._cv:
@@ -293,7 +308,7 @@ class Server:
             if need > self.adjoint_budget:
                 return self._finish(res, error=f"adjoint needs {need} bytes, budget {self.adjoint_budget}")
             with self._cv:
-                self._adj_q.append((req, res, need))
+                self._adj_q[req.cls].append((req, res, need))
                 self._cv.notify_all()
         else:
             self._finish(res, error=f"unknown request kind {req.kind!r}")
@@ -363,17 +378,17 @@ class Server:
                 self._cv.notify_all()
 
     # -- adjoint workers -------------------------------------------------------
-    def _adj_loop(self) -> None:
+    def _adj_loop(self, key) -> None:
         try:
-            stream = self._stream_factory()
+            stream = self._stream_factory(self._prio.get(key, 0))
+            q = self._adj_q[key]
             while True:
                 with self._cv:
-                    while not self._stop and not (self._adj_q and
-                                                  self._adj_q[0][2] <= self.adjoint_budget - self._adj_used):
+                    while not self._stop and not (q and q[0][2] <= self.adjoint_budget - self._adj_used):
                         self._cv.wait()
                     if self._stop:
                         return
-                    req, res, need = self._adj_q.popleft()
+                    req, res, need = q.popleft()
                     self._adj_used += need
                 res.t_admit = self.now()
                 err = None
@@ -408,6 +423,12 @@ class Server:
         if objs is None:
             sig = Signals(req.signals, spec.window, spec.im, self.precision, stream=stream)
             b = Batch(plan, req.values, req.x0, req.exc_index, stream=stream)
+            if self.reserve:   # grown buffers are fresh: upload the request again afterwards
+                max_sys, max_steps, max_samples = self.reserve
+                b.reserve(max_sys, max_steps)
+                b.set(req.values, req.x0, req.exc_index, stream=stream)
+                sig.update(np.zeros((1, int(max_samples))), stream=stream)
+                sig.update(req.signals, stream=stream)
             cache[id(spec)] = (sig, b)
         else:
             sig, b = objs
@@ -417,9 +438,11 @@ class Server:
                          sq_start=req.sq_start, stream=stream)
 
 
-def _torch_stream():
+def _torch_stream(priority: int = 0):
+    """A CUDA stream; lower priority numbers are scheduled first (torch clamps
+    to the device's range)."""
     import torch
-    return torch.cuda.Stream()
+    return torch.cuda.Stream(priority=priority)
 
 
 # ---- the served mixed stream ------------------------------------------------

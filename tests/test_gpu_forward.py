@@ -178,3 +178,26 @@ def test_forward_warp_sliced_chain(gpu, nd):
         np.testing.assert_array_equal(got[0], ost)
         np.testing.assert_array_equal(got[1], omx)
         np.testing.assert_array_equal(got[2], osq)
+
+
+def test_reserve_requires_inputs_again(gpu):
+    """Reserving grows the device buffers without keeping their contents: a
+    solve before the inputs are set again is refused (PASIF_ERR_STATE), and
+    after set a reused, resized batch equals a fresh one."""
+    from pasif_gb300 import _native as N
+    w = synth.chain8(n_sys=40, nsteps=302)
+    sig = Signals(w.signals, w.window, w.im, "fp32_kahan")
+    plan = Plan(w.pattern, "fp32_kahan", literals=False)
+    b = Batch(plan, w.values[:7], w.x0[:7], w.exc_index[:7])
+    b.reserve(4096, 200_000)
+    with pytest.raises(N.PasifError) as e:
+        b.forward(sig, w.h, 300)
+    assert e.value.code == N.ERR_STATE
+    with pytest.raises(N.PasifError):
+        b.adjoint(sig, w.h, 300, g_sq=np.ones(7), sq_comp=(0,))
+    b.set(w.values, w.x0, w.exc_index)               # resized to 40
+    b.forward(sig, w.h, 300, max_comp=(0,))
+    fresh = Batch(plan, w.values, w.x0, w.exc_index)
+    fresh.forward(sig, w.h, 300, max_comp=(0,))
+    for x, y in zip(b.get(), fresh.get()):
+        np.testing.assert_array_equal(x, y)

@@ -3,6 +3,7 @@ runner (no GPU): first-come-first-served admission by free slots and arena
 space, refusal of requests that can never fit, the adjoint memory budget,
 and latency bookkeeping."""
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -53,7 +54,7 @@ def make_server(capacity=8, arena=1000, budget=100, workers=2, runner=None, log=
     return S.Server({"a": spec}, capacity=capacity, arena_samples=arena, adjoint_budget=budget,
                     adjoint_workers=workers, pool_factory=lambda sp: FakePool(capacity, arena, sp.chunk, log),
                     adjoint_runner=runner or (lambda sp, rq, st: (rq.values * 3.0, rq.x0)),
-                    stream_factory=lambda: None), log
+                    stream_factory=lambda prio: None), log
 
 
 def req(rid, kind, n, nsteps=25, table=10):
@@ -143,6 +144,38 @@ def test_adjoint_errors():
     srv.submit(req(2, "adjoint", 1))
     with pytest.raises(RuntimeError, match="boom"):
         srv.wait(10.0)
+    srv.stop()
+
+
+def test_adjoint_classes_do_not_block_each_other():
+    """Each class has its own adjoint queue and workers: a cheap request is
+    served while long requests of another class are still running."""
+    spec = S.ClassSpec(PAT, 0.01, 0, None, (0,), chunk=10)
+    release = threading.Event()
+
+    def runner(sp, rq, stream):
+        if rq.cls == "slow":
+            release.wait(10.0)
+        return rq.values, rq.x0
+
+    srv = S.Server({"slow": spec, "fast": spec}, adjoint_budget=1 << 30, adjoint_workers=1,
+                   pool_factory=lambda sp: FakePool(8, 1000, sp.chunk, []), adjoint_runner=runner,
+                   stream_factory=lambda prio: None)
+    srv.start()
+    for i in range(3):
+        rq = req(i, "adjoint", 1)
+        rq.cls = "slow"
+        srv.submit(rq)
+    fast = req(9, "adjoint", 1)
+    fast.cls = "fast"
+    srv.submit(fast)
+    deadline = time.time() + 10.0
+    while np.isnan(srv.results()[9].t_done) and time.time() < deadline:
+        time.sleep(0.01)
+    assert not np.isnan(srv.results()[9].t_done)          # done while the slow class is still blocked
+    assert all(np.isnan(srv.results()[i].t_done) for i in range(3))
+    release.set()
+    assert srv.wait(10.0)
     srv.stop()
 
 

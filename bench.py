@@ -295,6 +295,43 @@ def main():
     # elementwise ratio is meaningless for gradient entries that are ~0)
     grel = np.max(np.abs(g32 - g64), axis=1) / np.maximum(np.max(np.abs(g64), axis=1), 1e-300)
 
+    # the other forward configurations: config 1 (1-DOF Duffing, 1024 systems x
+    # 1e5 steps) and config 4 (32-DOF banded, 2048 systems x 1e6 steps, the
+    # warp-sliced kernel), FP32-Kahan and FP64, amplitude error max|x_0| over
+    # the final half
+    def timed_forward(wl, prec):
+        pl = Plan(wl.pattern, prec)
+        sg = Signals(wl.signals, wl.window, wl.im, prec, stream=stream)
+        bt = Batch(pl, wl.values, wl.x0, wl.exc_index, stream=stream)
+        bt.forward(sg, wl.h, 64, stream=stream, **wl.forward_kwargs())   # warm (NVRTC)
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        bt.forward(sg, wl.h, wl.nsteps, stream=stream, **wl.forward_kwargs())
+        f1.record(stream)
+        torch.cuda.synchronize()
+        _, mx, _ = bt.get(stream=stream)
+        return wl.n_sys * wl.nsteps / (f0.elapsed_time(f1) * 1e-3), mx, bt.kernel_info()
+
+    other = {}
+    for name, wl in (("config1_duffing", synth.duffing()), ("config4_banded32", synth.banded32())):
+        r32, m32, k32 = timed_forward(wl, "fp32_kahan")
+        r64, m64, k64 = timed_forward(wl, "fp64")
+        # some undamped, forced banded systems diverge over 1e6 steps (in both
+        # precisions): the error is taken over the systems finite in both
+        fin = np.isfinite(m32).all(axis=1) & np.isfinite(m64).all(axis=1)
+        err = np.abs(m32[fin] - m64[fin]) / np.maximum(np.abs(m64[fin]), 1e-300)
+        other[name] = {"workload": wl.name, "systems": wl.n_sys, "rk4_steps": wl.nsteps, "states": wl.pattern.n,
+                       "fp32_kahan": {"value": r32, "unit": UNIT, "registers": k32["registers"]},
+                       "fp64": {"value": r64, "unit": UNIT},
+                       "speedup_fp32_kahan": r32 / r64,
+                       "flops_per_system_step": wl.flops_per_system_step(),
+                       "fp32_kahan_tflops": r32 * wl.flops_per_system_step() / 1e12,
+                       "max_rel_err_amplitude_fp32_kahan_vs_fp64": float(err.max()) if err.size else None,
+                       "median_rel_err_amplitude": float(np.median(err)) if err.size else None,
+                       "diverged_systems": {"fp32_kahan": int((~np.isfinite(m32).all(axis=1)).sum()),
+                                            "fp64": int((~np.isfinite(m64).all(axis=1)).sum())}}
+
     # served mixed stream: Poisson 200 req/s, 70/30 forward/adjoint, 1-4096
     # systems of DOF 1..64, 1e4-2e5 steps (continuous batching, p50/p99)
     served = None
@@ -335,6 +372,7 @@ def main():
                             "median_rel_err_grad": float(np.median(grel)),
                             "rel_err_definition": "per system max|g32-g64| / max|g64| over its values",
                             "bound": 1e-5},
+                "other_configs": other,
                 "serving": served,
                 "wall_s_timed_region": t_wall}
         if world == 1:

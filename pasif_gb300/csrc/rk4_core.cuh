@@ -9,9 +9,10 @@
 // round-to-nearest intrinsic (__fma_rn, __dmul_rn, ...): the compiler may not
 // fuse or reorder them, and the operation order is the canonical one of the
 // CPU oracle (per destination: CSR row of K, then Gamma, Lambda, Psi entries
-// in COO order, then forcing; fma-folded from +0).  This is the order the
-// reference's kernels sum in, minus its atomicAdd nondeterminism
-// (src/kernels.cu:22-64, src/__GpuDriver.cu:785-838).
+// in COO order, then forcing, dealt in turn to two partial sums that start
+// as the product of their first term, fold the rest with fma and are added).
+// The reference's kernels sum the same terms with atomicAdd, in no fixed
+// order (src/kernels.cu:22-64, src/__GpuDriver.cu:785-838).
 #pragma once
 #include "pk_args.h"
 

@@ -161,6 +161,7 @@ class PASIf(_GpuDriver):
             vecInitialConditions), "The number of Systems in the input vectors must be the same."
         self._check(vecM, vecB, vecK, vecGamma, vecLambda, vecForcePattern, vecInitialConditions)
         self.numberOfSystems = len(vecM)
+        self._user_systems = (list(vecM), list(vecB), list(vecK), list(vecGamma), list(vecLambda))
         G, M, Bm, Km, (Gam, Lam), F, IC = self._unfold(vecM, vecB, vecK, [vecGamma, vecLambda], vecForcePattern,
                                                        vecInitialConditions)
         self.globalSystemSize = G
@@ -184,6 +185,24 @@ class PASIf(_GpuDriver):
         self._setFwdInitialConditions(IC)
         self.systemSet = True
         self._allocateSystemOnDevice()
+
+    def setGeneratedJacobian(self, terminals=None):
+        """setJacobian with backward systems generated from the systems given
+        to setSystems (pasif_gb300.adjoint_system; the role of the external
+        modelling tool).  terminals[i]: dL/dq(T) of system i (default 0).
+        Returns, per system, the parameter of each gradient accumulator (the
+        entries of -M^-1 (B + K) in CSR order, then Gamma, then Lambda)."""
+        from .adjoint_system import jacobian_inputs
+        if not self.systemSet:
+            raise ValueError("The system must be set before the jacobian")
+        ins, params = [], []
+        for i, (M, B, K, G, L) in enumerate(zip(*self._user_systems)):
+            t = None if terminals is None else terminals[i]
+            j, p = jacobian_inputs(M, B, K, G, L, terminal=t)
+            ins.append(j)
+            params.append(p)
+        self.setJacobian(*[list(z) for z in zip(*ins)])
+        return params
 
     def setJacobian(self, vecM, vecB, vecK, vecGamma, vecLambda, vecForcePattern, vecInitialConditions, vecPsi):
         self.jacobianSet = False

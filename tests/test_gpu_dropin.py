@@ -75,6 +75,30 @@ def test_amplitudes_bit_exact(gpu):
     np.testing.assert_array_equal(np.asarray(p.getAmplitudes()), ref)
 
 
+def test_amplitudes_large_block_warp_sliced(gpu):
+    """A 30-state user system next to a small one: the driver's split gives it
+    its own block, solved by the warp-sliced kernel (from 28 states in FP32,
+    24 in FP64), and the amplitudes equal the oracle's on the concatenated
+    system (bit for bit in FP64, within 1e-5 in FP32-Kahan)."""
+    rng = np.random.default_rng(25)
+    E, L = 2, 120
+    exc = [np.sin(0.05 * (e + 1) * np.arange(L)) + 0.1 * rng.standard_normal(L) for e in range(E)]
+    for precision in ("fp64", "fp32_kahan"):
+        p = PASIf(exc, 64, 150, precision=precision)
+        systems = [random_user_system(np.random.default_rng(26), 30), probe_system()]
+        p.setSystems(*[list(z) for z in zip(*systems)])
+        got = np.asarray(p.getAmplitudes())
+        K, Gam, Lam, F, IC = p.getMatrices()
+        csr = K.tocsr(); csr.sort_indices()
+        pat, vals = oracle_system(csr, Gam, Lam, F)
+        if precision == "fp64":
+            ref = O.get_amplitudes(pat, vals, IC, np.asarray(exc), 1 / 64, 150)
+            np.testing.assert_array_equal(got, ref)
+        else:
+            ref64 = ref
+            np.testing.assert_allclose(got, ref64, rtol=1e-5, atol=1e-7)
+
+
 def test_amplitudes_with_interpolation_matrix(gpu):
     rng = np.random.default_rng(22)
     W = 8
@@ -139,6 +163,33 @@ def test_gradient_reference_semantics(gpu):
     ref2 = np.concatenate([O.get_gradient(fpat, fvals, IC, bpat, bvals, ref[e * 12:(e + 1) * 12],
                                           np.asarray(exc)[e:e + 1], 1 / 16, N) for e in range(E)])
     np.testing.assert_array_equal(got2, ref2)
+
+
+def test_gradient_with_generated_jacobian(gpu):
+    """getGradient with backward systems generated from the forward systems
+    (setGeneratedJacobian) equals the oracle's _getGradient on the same
+    preprocessed backward system, bit for bit; the accumulators list the
+    parameters of -M^-1 (B + K), Gamma, Lambda."""
+    rng = np.random.default_rng(27)
+    E, L = 2, 160
+    exc = [np.sin(0.07 * (e + 1) * np.arange(L)) + 0.1 * rng.standard_normal(L) for e in range(E)]
+    N = 140
+    p = PASIf(exc, 32, N)
+    sysl = [random_user_system(np.random.default_rng(28), 3), random_user_system(np.random.default_rng(29), 2)]
+    p.setSystems(*[list(z) for z in zip(*sysl)])
+    terminals = [rng.normal(size=3), rng.normal(size=2)]
+    params = p.setGeneratedJacobian(terminals)
+    assert [len(x) for x in params] == [p.jacobian_initialConditions.size - 5 - len(params[1]), len(params[1])]
+    got = np.asarray(p.getGradient())
+    K, Gam, Lam, F, IC = p.getMatrices()
+    csr = K.tocsr(); csr.sort_indices()
+    fpat, fvals = oracle_system(csr, Gam, Lam, F)
+    bcsr = (p.jacobian_B + p.jacobian_K).tocsr(); bcsr.sort_indices()
+    bpat, bvals = oracle_system(bcsr, p.jacobian_Gamma, p.jacobian_Lambda, p.jacobian_forcePattern, p.jacobian_Psi,
+                                n_sp=fpat.n)
+    a0 = np.asarray(p.jacobian_initialConditions, float)
+    ref = O.get_gradient(fpat, fvals, IC, bpat, bvals, a0, np.asarray(exc), 1 / 32, N)
+    np.testing.assert_array_equal(got, ref)
 
 
 def test_error_behaviour(gpu):

@@ -229,6 +229,7 @@ class Server:
         self._n_adj_workers = int(adjoint_workers)
         self._plans = {}
         self._tls = threading.local()     # per adjoint worker: reused batch and signal table per class
+        self._worker_objs = {}            # (class, worker) -> (signals, batch) reserved by warm()
         self._errors = []
         self.t0 = self.clock()
         self.chunks = collections.Counter()
@@ -253,8 +254,10 @@ class Server:
             return self._pools[key]
 
     def warm(self, keys=None, adjoint: bool = True) -> None:
-        """Make the pools and compile the kernels of the given classes now
-        (compilation is otherwise paid by the first request of a class)."""
+        """Make the pools, compile the kernels of the given classes and (with
+        `reserve`) size every adjoint worker's batch and signal table now:
+        compilation and device allocation (which synchronises the device)
+        are otherwise paid while requests are in flight."""
         for k in (self.specs if keys is None else keys):
             self._pool(k)
             if adjoint:
@@ -262,13 +265,21 @@ class Server:
                 n, P = spec.pattern.n, spec.pattern.P
                 rq = Request(-1, "adjoint", k, np.zeros((1, P)), np.zeros((1, n)), np.zeros(1, np.int32),
                              np.zeros((1, 8)), 4, 0, 0)
-                self._adjoint_runner(spec, rq, None)
+                if self._n_adj_workers == 0:
+                    continue
+                if self.reserve and self._adjoint_runner == self._run_adjoint:
+                    for i in range(self._n_adj_workers):
+                        self._worker_objs[(k, i)] = self._adjoint_objects(spec, rq, None)
+                    sig, b = self._worker_objs[(k, 0)]   # compile the adjoint kernel
+                    b.adjoint(sig, spec.h, rq.nsteps, g_sq=np.ones(1), sq_comp=spec.positions, sq_start=0)
+                else:
+                    self._adjoint_runner(spec, rq, None)
 
     def start(self) -> None:
         self.t0 = self.clock()
         for key in self.specs:
             for i in range(self._n_adj_workers):
-                t = threading.Thread(target=self._adj_loop, args=(key,), daemon=True, name=f"adjoint-{key}-{i}")
+                t = threading.Thread(target=self._adj_loop, args=(key, i), daemon=True, name=f"adjoint-{key}-{i}")
                 self._threads.append(t)
                 t.start()
 
@@ -378,8 +389,11 @@ class Server:
                 self._cv.notify_all()
 
     # -- adjoint workers -------------------------------------------------------
-    def _adj_loop(self, key) -> None:
+    def _adj_loop(self, key, index: int = 0) -> None:
         try:
+            objs = self._worker_objs.get((key, index))
+            if objs is not None:   # reserved by warm()
+                self._tls.__dict__.setdefault("objs", {})[id(self.specs[key])] = objs
             stream = self._stream_factory(self._prio.get(key, 0))
             q = self._adj_q[key]
             while True:
@@ -411,6 +425,20 @@ class Server:
         batch and one signal table per class and reuses their device buffers:
         a device allocation or free per request would synchronise the whole
         device and stall every other request in flight."""
+        cache = self._tls.__dict__.setdefault("objs", {})
+        objs = cache.get(id(spec))
+        if objs is None:
+            sig, b = cache[id(spec)] = self._adjoint_objects(spec, req, stream)
+        else:
+            sig, b = objs
+            sig.update(req.signals, stream=stream)
+            b.set(req.values, req.x0, req.exc_index, stream=stream)
+        return b.adjoint(sig, spec.h, req.nsteps, g_sq=np.ones(req.n_sys), sq_comp=spec.positions,
+                         sq_start=req.sq_start, stream=stream)
+
+    def _adjoint_objects(self, spec: ClassSpec, req: Request, stream):
+        """A signal table and a batch of the class (plan shared, no literals),
+        holding `req`, with buffers reserved for the largest request."""
         from .batch import Batch, Plan, Signals
         with self._cv:
             plan = self._plans.get(id(spec))
@@ -418,24 +446,15 @@ class Server:
             plan = Plan(spec.pattern, self.precision, literals=False)
             with self._cv:
                 plan = self._plans.setdefault(id(spec), plan)
-        cache = self._tls.__dict__.setdefault("objs", {})
-        objs = cache.get(id(spec))
-        if objs is None:
-            sig = Signals(req.signals, spec.window, spec.im, self.precision, stream=stream)
-            b = Batch(plan, req.values, req.x0, req.exc_index, stream=stream)
-            if self.reserve:   # grown buffers are fresh: upload the request again afterwards
-                max_sys, max_steps, max_samples = self.reserve
-                b.reserve(max_sys, max_steps)
-                b.set(req.values, req.x0, req.exc_index, stream=stream)
-                sig.update(np.zeros((1, int(max_samples))), stream=stream)
-                sig.update(req.signals, stream=stream)
-            cache[id(spec)] = (sig, b)
-        else:
-            sig, b = objs
-            sig.update(req.signals, stream=stream)
+        sig = Signals(req.signals, spec.window, spec.im, self.precision, stream=stream)
+        b = Batch(plan, req.values, req.x0, req.exc_index, stream=stream)
+        if self.reserve:   # grown buffers are fresh: upload the request again afterwards
+            max_sys, max_steps, max_samples = self.reserve
+            b.reserve(max_sys, max_steps)
             b.set(req.values, req.x0, req.exc_index, stream=stream)
-        return b.adjoint(sig, spec.h, req.nsteps, g_sq=np.ones(req.n_sys), sq_comp=spec.positions,
-                         sq_start=req.sq_start, stream=stream)
+            sig.update(np.zeros((1, int(max_samples))), stream=stream)
+            sig.update(req.signals, stream=stream)
+        return sig, b
 
 
 def _torch_stream(priority: int = 0):

@@ -338,10 +338,16 @@ def main():
 
     # served mixed stream: Poisson 200 req/s, 70/30 forward/adjoint, 1-4096
     # systems of DOF 1..64, 1e4-2e5 steps (continuous batching, p50/p99)
+    # (in its own process, as a server runs: a fresh CUDA context and host
+    # threads of its own)
     served = None
     if args.serve > 0 and rank == 0:
-        from pasif_gb300 import serve
-        served = serve.run(rate=200.0, duration=args.serve, seed=5)
+        pr = subprocess.run([sys.executable, "-m", "pasif_gb300.serve", "--rate", "200", "--duration",
+                             str(args.serve), "--seed", "5"], capture_output=True, text=True, cwd=ROOT,
+                            env=dict(os.environ, PYTHONPATH=ROOT))
+        lines = [l for l in pr.stdout.splitlines() if l.startswith("{")]
+        served = json.loads(lines[-1]) if pr.returncode == 0 and lines else {
+            "error": f"serve exited {pr.returncode}: {pr.stderr[-400:]}"}
 
     # roofline: algorithmic FLOPs per launch / launch time vs the measured FMA peak
     flops_ss = w.pattern.flops_per_step()

@@ -23,13 +23,15 @@ from . import synth
 
 
 def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, capacity=16384,
-        arena_samples=1 << 25, adjoint_budget=32 << 30, adjoint_workers=3, check=6, log=None) -> dict:
+        arena_samples=1 << 25, adjoint_budget=48 << 30, adjoint_workers=None, check=6, log=None) -> dict:
     dofs = tuple(dofs or synth.SERVED_DOFS)
     specs = S.served_specs(dofs)
     stream = synth.served_stream(rate, duration, seed, dofs=dofs)
     t = time.perf_counter()
     reqs = [(sr.arrival, S.make_request(sr, specs[sr.dof])) for sr in stream]
     t_gen = time.perf_counter() - t
+    if adjoint_workers is None:   # more workers where one adjoint is long and uses few SMs
+        adjoint_workers = {d: 6 if s.pattern.n >= 60 else 4 if s.pattern.n >= 24 else 2 for d, s in specs.items()}
     srv = S.Server(specs, precision, capacity, arena_samples, adjoint_budget, adjoint_workers,
                    reserve=(4096, 200_000, 4 * 200_003))
     t = time.perf_counter()

@@ -226,7 +226,10 @@ class Server:
         self._outstanding = 0
         self._stop = False
         self._threads = []
-        self._n_adj_workers = int(adjoint_workers)
+        # adjoint workers per class: an int, or a dict class -> int (long adjoints of
+        # large systems each run latency-bound on a few SMs: more of them at once)
+        self._adj_workers = (dict(adjoint_workers) if isinstance(adjoint_workers, dict)
+                             else {k: int(adjoint_workers) for k in self.specs})
         self._plans = {}
         self._tls = threading.local()     # per adjoint worker: reused batch and signal table per class
         self._worker_objs = {}            # (class, worker) -> (signals, batch) reserved by warm()
@@ -265,10 +268,11 @@ class Server:
                 n, P = spec.pattern.n, spec.pattern.P
                 rq = Request(-1, "adjoint", k, np.zeros((1, P)), np.zeros((1, n)), np.zeros(1, np.int32),
                              np.zeros((1, 8)), 4, 0, 0)
-                if self._n_adj_workers == 0:
+                nw = self._adj_workers.get(k, 0)
+                if nw == 0:
                     continue
                 if self.reserve and self._adjoint_runner == self._run_adjoint:
-                    for i in range(self._n_adj_workers):
+                    for i in range(nw):
                         self._worker_objs[(k, i)] = self._adjoint_objects(spec, rq, None)
                     sig, b = self._worker_objs[(k, 0)]   # compile the adjoint kernel
                     b.adjoint(sig, spec.h, rq.nsteps, g_sq=np.ones(1), sq_comp=spec.positions, sq_start=0)
@@ -278,7 +282,7 @@ class Server:
     def start(self) -> None:
         self.t0 = self.clock()
         for key in self.specs:
-            for i in range(self._n_adj_workers):
+            for i in range(self._adj_workers.get(key, 0)):
                 t = threading.Thread(target=self._adj_loop, args=(key, i), daemon=True, name=f"adjoint-{key}-{i}")
                 self._threads.append(t)
                 t.start()

@@ -219,13 +219,10 @@ def main():
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
         barrier()
-    kernel_s = sum(e0.elapsed_time(e1) for e0, e1 in evs) * 1e-3
-    t = torch.tensor([kernel_s], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    kernel_s = float(t.item())
+    from pasif_gb300.replicas import job_rate, max_over_ranks
+    kernel_s = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in evs) * 1e-3, dist, "cuda")
     sys_steps = w.n_sys * w.nsteps
-    value = world * sys_steps * args.steps / kernel_s
+    value = job_rate(sys_steps * args.steps, world, kernel_s)
     ms_per_step = 1e3 * kernel_s / args.steps
     st32, _, _ = batch.get(stream=stream)
 

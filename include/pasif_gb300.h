@@ -251,7 +251,9 @@ int pasif_pool_create(pasif_pool** out, const pasif_pattern* pattern, int precis
 int pasif_pool_destroy(pasif_pool* p);
 /* Host arrays: values[n_sys][P], x0[n_sys][n], exc_index[n_sys],
  * signals[n_exc][len]; integrates nsteps from step 0.  PASIF_ERR_STATE when
- * slots or arena space are short (retry after a harvest). */
+ * slots or arena space are short (retry after a harvest); PASIF_ERR_INVALID
+ * when the request can never fit (more systems than slots, a table larger
+ * than the arena). */
 int pasif_pool_admit(pasif_pool* p, int n_sys, const double* values, const double* x0,
                      const int* exc_index, const double* signals, int n_exc, int len, int nsteps,
                      int max_start, int sq_start, int* request_id);
@@ -260,7 +262,8 @@ int pasif_pool_launch(pasif_pool* p);
 /* Waits for the pool's stream; lists requests whose slots have all finished. */
 int pasif_pool_poll(pasif_pool* p, int* finished, int capacity, int* n_finished);
 /* Results of a finished request (state[n_sys][n], max[n_sys][n_max],
- * sq[n_sys]; any may be NULL); frees its slots and arena space. */
+ * sq[n_sys]; any may be NULL); frees its slots and arena space.
+ * PASIF_ERR_STATE (nothing freed) while any of its slots has steps left. */
 int pasif_pool_harvest(pasif_pool* p, int request_id, double* state, double* max, double* sq);
 int pasif_pool_info(pasif_pool* p, int* free_slots, long long* free_arena, int* active);
 /* Compile (no GPU needed) the pool chunk kernel a pool of this plan would

@@ -236,6 +236,7 @@ int Pool::admit(int n_sys, const double* values, const double* x0, const int* ex
     for (int i = 0; i < n_sys; ++i)
         if (exc_index[i] < 0 || exc_index[i] >= n_exc) { *err = "excitation index out of range"; return 1; }
     const long long table = (long long)n_exc * len;
+    if (n_sys > C_ || table > S_) { *err = "request larger than the pool (slots or signal arena)"; return 1; }
     if ((int)free_.size() < n_sys) { *err = "pool full"; return 5; }
     const long long off = arena_alloc(table);
     if (off < 0) { *err = "signal arena full"; return 5; }
@@ -332,6 +333,12 @@ int Pool::harvest(int req_id, double* state, double* max, double* sq, std::strin
     auto it = reqs_.find(req_id);
     if (it == reqs_.end()) { *err = "unknown request"; return 1; }
     const PoolRequest& r = it->second;
+    // finished = every slot at 0 remaining steps, read after the last chunk
+    // (a request harvested early would free slots a chunk may still advance)
+    PL_CUDA(cudaMemcpyAsync(remain_host_, remain_.p, sizeof(int) * C_, cudaMemcpyDeviceToHost, st_), "cudaMemcpyAsync");
+    PL_CUDA(cudaStreamSynchronize(st_), "cudaStreamSynchronize");
+    for (int s : r.slots)
+        if (remain_host_[s] > 0) { *err = "request not finished (poll until it is listed)"; return 5; }
     const int n = plan_->pat.n, m = r.n_sys;
     const bool f32 = plan_->precision != kFP64;
     const size_t so = 0, oo = (sizeof(double) * (size_t)m * n + 15) & ~(size_t)15;

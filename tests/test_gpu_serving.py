@@ -72,16 +72,23 @@ def test_pool_requests_equal_alone(gpu, prec, seed, W, slicing):
 def test_pool_refuses_when_full(gpu):
     w = synth.duffing(n_sys=8, nsteps=100)
     pool = S.Pool(w.pattern, "fp32_kahan", 2, w.im, w.h, (0,), (), capacity=8, arena_samples=3 * 102, chunk=50)
+    from pasif_gb300 import _native as N
     a = pool.admit(w.values, w.x0, np.zeros(8, np.int32), w.signals[:1], 100)
     assert a is not None
     assert pool.admit(w.values[:1], w.x0[:1], [0], w.signals[:1], 100) is None      # no free slot
     pool.launch()
+    with pytest.raises(N.PasifError) as e:                                          # 50 of 100 steps done
+        pool.harvest(a, 8)
+    assert e.value.code == N.ERR_STATE
     pool.launch()
     assert pool.poll() == [a]
     pool.harvest(a, 8)
     b = pool.admit(w.values[:4], w.x0[:4], [0, 0, 0, 0], w.signals[:3], 100)
     assert b is not None
     assert pool.admit(w.values[:1], w.x0[:1], [0], w.signals[:1], 100) is None      # arena full
+    with pytest.raises(N.PasifError) as e:                                          # can never fit
+        pool.admit(np.tile(w.values, (2, 1)), np.tile(w.x0, (2, 1)), np.zeros(16, np.int32), w.signals[:1], 100)
+    assert e.value.code == N.ERR_INVALID
 
 
 def small_stream(seed, n_req=24):

@@ -105,6 +105,7 @@ _SIGS = {
     "pasif_signals_update": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
     "pasif_batch_resize": (C.c_int, [_vp, C.c_int]),
     "pasif_batch_reserve": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "pasif_batch_set_adjoint_storage": (C.c_int, [_vp, C.c_longlong]),
     "pasif_batch_create": (C.c_int, [C.POINTER(_vp), _vp, C.c_int]),
     "pasif_batch_destroy": (C.c_int, [_vp]),
     "pasif_batch_set": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, _vp]),

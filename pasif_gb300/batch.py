@@ -33,8 +33,10 @@ class Plan:
                  slicing=None):
         """literals=False: the specialised kernels load every value, so one
         compiled kernel serves every batch of the plan (serving).
-        slicing: None = warp-sliced kernels from n >= 28 (FP32) / 24 (FP64), True = always,
-        False = never (thread per system)."""
+        slicing: None = warp-sliced kernels where they are faster on GB300
+        (forward: FP32 from n >= 28, FP64 from n >= 8, or n >= 3 for batches
+        up to 8192 systems; adjoint: FP32 from n >= 5, FP64 from n >= 2),
+        True = always, False = never (thread per system)."""
         self.pattern = pattern
         self.precision = _prec(precision)
         self._c = pattern.to_c()
@@ -139,6 +141,12 @@ class Batch:
         """Size the device buffers for forward / adjoint solves of up to n_sys
         instances and nsteps steps (later calls then allocate nothing)."""
         N.check(N.lib.pasif_batch_reserve(self.handle, int(n_sys), int(nsteps)))
+
+    def adjoint_storage(self, nbytes: int):
+        """Device memory the exact adjoint may hold for the whole forward
+        trajectory (default 16 GiB; 0 always recomputes from checkpoints).
+        Results do not depend on it; set it before reserve()."""
+        N.check(N.lib.pasif_batch_set_adjoint_storage(self.handle, int(nbytes)))
 
     def set(self, values, x0, exc_index, stream=None):
         """New inputs; a different instance count resizes the batch (its

@@ -360,6 +360,13 @@ int pasif_batch_reserve(pasif_batch* b, int n_sys, int nsteps) {
     });
 }
 
+int pasif_batch_set_adjoint_storage(pasif_batch* b, long long bytes) {
+    if (!b || !b->b) return fail(PASIF_ERR_INVALID, "null batch");
+    if (bytes < 0) return fail(PASIF_ERR_INVALID, "negative storage limit");
+    b->b->adj_store_limit = (size_t)bytes;
+    return 0;
+}
+
 int pasif_batch_create(pasif_batch** out, pasif_plan* plan, int n_sys) {
     return guard([&] {
         if (!out || !plan) return fail(PASIF_ERR_INVALID, "null handle");
@@ -617,7 +624,7 @@ int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys, 
         key.kahan = p->p->precision == pasif::kFP32Kahan;
         key.max_mask = max_mask;
         key.sq_mask = sq_mask;
-        key.slices = p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0);
+        key.slices = p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0, n_sys);
         if (window < 0 || (window > 0 && (!im || (window & (window - 1)))))
             return fail(PASIF_ERR_INVALID, "window must be 0 or a power of two with weights");
         key.window = window;

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 
@@ -163,7 +164,7 @@ int Batch::reserve(int n_sys, int nsteps, std::string* err) {
     PK_CUDA(out_max.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(out_sq.ensure(Bn * rs), "cudaMalloc");
     PK_CUDA(ckpt.ensure(Bn * 2 * n * nck * rs), "cudaMalloc");
-    PK_CUDA(buf.ensure(Bn * n * C * rs), "cudaMalloc");
+    PK_CUDA(buf.ensure(Bn * n * (adj_stores((int)Bn, nsteps) ? (size_t)nsteps + 1 : C) * rs), "cudaMalloc");
     PK_CUDA(pbar.ensure(Bn * P * sizeof(double)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(gfin.ensure(Bn * n * rs), "cudaMalloc");
@@ -320,6 +321,68 @@ static void fill_fwd(pk::FwdArgs<R>& a, Batch& bt, const Signals& sig, double h,
     a.sq_mask = sm;
 }
 
+// Threads per block of a thread-per-system forward: 128, halved down to 32
+// while the batch would fill fewer blocks than the device has SMs, so that a
+// small batch spreads its warps over more SMs (GB300: +8 % FP32, +13 % FP64 on
+// 1024 one-DOF systems; +15 % FP64 on 4096 16-state chains).
+static int tps_block(int B) {
+    if (const char* e = std::getenv("PASIF_TPS_BLOCK")) {   // tuning override: 32, 64, 96 or 128
+        const int v = std::atoi(e);
+        if (v >= 32 && v <= 128 && v % 32 == 0) return v;
+    }
+    static const int sms = [] {
+        int d = 0, s = 0;
+        if (cudaGetDevice(&d) != cudaSuccess || cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, d) != cudaSuccess)
+            return 0;
+        return s;
+    }();
+    int block = 128;
+    while (block > 32 && (B + block - 1) / block < sms) block /= 2;
+    return block;
+}
+
+bool Batch::fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long long sm, bool with_traj,
+                       JitKernel* k, std::string* jerr) {
+    const Pattern& pat = plan->pat;
+    if (plan->generic_only || pat.n > kWsMaxN) {
+        *jerr = "no specialised forward kernel for this plan";
+        return false;
+    }
+    const bool f = f32();
+    FwdKernelKey key;
+    key.f32 = f;
+    key.kahan = plan->precision == kFP32Kahan;
+    key.max_mask = mm;
+    key.sq_mask = sm;
+    key.traj = with_traj;
+    key.block = tps_block(B);
+    key.window = (int)sig.w;
+    key.wn.assign(sig.im_host.begin(), sig.im_host.begin() + sig.w);
+    key.wc.assign(sig.im_host.begin() + sig.w, sig.im_host.end());
+    key.slices = plan->slicing < 0 ? 0 : ws_slices(pat, f, plan->slicing > 0, B);
+    return get_fwd_kernel(pat, lit, key, k, jerr);
+}
+
+cudaError_t Batch::launch_fwd_jit(const JitKernel& k, const Signals& sig, double h, int step0, int nsteps,
+                                  const Reducers& red, unsigned long long mm, unsigned long long sm, int traj_every,
+                                  long long traj_slots, void* state_p, void* traj_p, cudaStream_t st) {
+    const dim3 grid((unsigned)((B + k.per_block - 1) / k.per_block));
+    if (f32()) {
+        pk::FwdArgs<float> a;
+        fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
+        a.state = static_cast<float*>(state_p);
+        a.traj = static_cast<float*>(traj_p);
+        void* args[] = {&a};
+        return cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
+    }
+    pk::FwdArgs<double> a;
+    fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
+    a.state = static_cast<double*>(state_p);
+    a.traj = static_cast<double*>(traj_p);
+    void* args[] = {&a};
+    return cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
+}
+
 int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Reducers& red, int traj_every,
                    long long traj_slots, cudaStream_t st, std::string* err) {
     const Pattern& pat = plan->pat;
@@ -345,41 +408,17 @@ int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Re
     if (B == 0) { last_kind = kNone; return 0; }
     PK_CUDA(cudaMemcpyAsync(state.p, x0.p, (size_t)B * n * rs, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
     const bool kahan = plan->precision == kFP32Kahan;
-    if (!plan->generic_only && n <= kWsMaxN) {
-        FwdKernelKey key;
-        key.f32 = f;
-        key.kahan = kahan;
-        key.max_mask = mm;
-        key.sq_mask = sm;
-        key.traj = traj_every > 0;
-        key.block = 128;
-        key.window = (int)sig.w;
-        key.wn.assign(sig.im_host.begin(), sig.im_host.begin() + sig.w);
-        key.wc.assign(sig.im_host.begin() + sig.w, sig.im_host.end());
-        key.slices = plan->slicing < 0 ? 0 : ws_slices(pat, f, plan->slicing > 0);
-        JitKernel k;
-        std::string jerr;
-        if (get_fwd_kernel(pat, lit, key, &k, &jerr)) {
-            dim3 grid((unsigned)((B + k.per_block - 1) / k.per_block));
-            cudaError_t e;
-            if (f) {
-                pk::FwdArgs<float> a;
-                fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
-                void* args[] = {&a};
-                e = cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
-            } else {
-                pk::FwdArgs<double> a;
-                fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
-                void* args[] = {&a};
-                e = cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
-            }
-            PK_CUDA(e, "specialised forward kernel launch");
-            last_kind = kSpecialised;
-            last_jit = k;
-            return 0;
-        }
-        last_jit_error = jerr;
+    JitKernel k;
+    std::string jerr;
+    if (fwd_kernel(sig, mm, sm, traj_every > 0, &k, &jerr)) {
+        PK_CUDA(launch_fwd_jit(k, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots, state.p,
+                               traj_every > 0 ? traj.p : nullptr, st),
+                "specialised forward kernel launch");
+        last_kind = kSpecialised;
+        last_jit = k;
+        return 0;
     }
+    if (!plan->generic_only) last_jit_error = jerr;
     PK_CUDA(scratch.ensure(Bn * 6 * (size_t)n * rs), "cudaMalloc");
     cudaError_t e;
     if (f) {
@@ -449,8 +488,24 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     const int nck = nsteps > 0 ? (nsteps + C - 1) / C : 0;
     const size_t rs = rsize();
     const size_t Bn = (size_t)B;
-    PK_CUDA(ckpt.ensure(Bn * 2 * n * (size_t)(nck > 0 ? nck : 1) * rs), "cudaMalloc");
-    PK_CUDA(buf.ensure(Bn * (size_t)n * (size_t)C * rs), "cudaMalloc");
+    JitKernel jk;
+    std::string jerr;
+    const int slices = plan->slicing < 0 ? 0 : ws_slices_adjoint(pat, f, plan->slicing > 0);
+    const bool jit = !plan->generic_only &&
+                     get_adj_kernel(pat, lit, f, plan->precision == kFP32Kahan, g_sq ? sm : 0ull, slices, &jk, &jerr);
+    if (!jit && !plan->generic_only) last_jit_error = jerr;
+    // stored trajectory (specialised kernels, within adj_store_limit): the
+    // batch's forward kernel writes the state before every step once
+    JitKernel fk;
+    std::string ferr;
+    const bool stored = jit && adj_stores(B, nsteps) && fwd_kernel(sig, 0ull, 0ull, true, &fk, &ferr);
+    const size_t vec = Bn * (size_t)n * rs;
+    if (stored) {
+        PK_CUDA(buf.ensure((size_t)(nsteps + 1) * vec), "cudaMalloc");
+    } else {
+        PK_CUDA(ckpt.ensure(Bn * 2 * n * (size_t)(nck > 0 ? nck : 1) * rs), "cudaMalloc");
+        PK_CUDA(buf.ensure(Bn * (size_t)n * (size_t)C * rs), "cudaMalloc");
+    }
     PK_CUDA(pbar.ensure(Bn * (size_t)(P > 0 ? P : 1) * sizeof(double)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     if (g_final) {
@@ -460,6 +515,13 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     if (g_sq) {
         int rc = upload_conv(g_sq, B, f, memory, gsq, adj_stage, st, err);
         if (rc) return rc;
+    }
+    if (stored) {   // slot 0 = x0; slots 1..nsteps from the forward kernel (state in dx0, replaced later)
+        PK_CUDA(cudaMemcpyAsync(buf.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
+        PK_CUDA(cudaMemcpyAsync(dx0.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
+        PK_CUDA(launch_fwd_jit(fk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, 1, nsteps, dx0.p,
+                               static_cast<char*>(buf.p) + vec, st),
+                "trajectory forward kernel launch");
     }
     cudaError_t e;
 #define PK_FILL_ADJ(R_)                                               \
@@ -486,13 +548,8 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     a.nck = nck;                                                      \
     a.kahan = plan->precision == kFP32Kahan ? 1 : 0;                  \
     a.sq_start = red.sq_start;                                        \
-    a.sq_mask = g_sq ? sm : 0ull;
-    JitKernel jk;
-    std::string jerr;
-    const int slices = plan->slicing < 0 ? 0 : ws_slices_adjoint(pat, f, plan->slicing > 0);
-    const bool jit = !plan->generic_only &&
-                     get_adj_kernel(pat, lit, f, plan->precision == kFP32Kahan, g_sq ? sm : 0ull, slices, &jk, &jerr);
-    if (!jit && !plan->generic_only) last_jit_error = jerr;
+    a.sq_mask = g_sq ? sm : 0ull;                                     \
+    a.stored = stored ? 1 : 0;
     const dim3 grid((unsigned)(jit ? (B + jk.per_block - 1) / jk.per_block : (B + 127) / 128));
     if (jit && plan->precision == kFP32Kahan) PK_CUDA(lamc.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     // Specialised kernels over many blocks: forward segments and backward chunk
@@ -510,7 +567,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
             a.phase = 0;
             return cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
         }
-        for (int t0 = 0; t0 < nsteps; t0 += per * C) {
+        for (int t0 = 0; t0 < (stored ? 0 : nsteps); t0 += per * C) {   // stored: no forward segments
             a.phase = 1;
             a.t_begin = t0;
             a.t_end = std::min(nsteps, t0 + per * C);

@@ -19,6 +19,8 @@ enum KernelKind { kNone = 0, kGeneric = 1, kSpecialised = 2 };
 
 // Steps per launch of a split exact adjoint (forward segments, backward chunk groups).
 constexpr int kAdjLaunchSteps = 2048;
+// Default device memory an exact adjoint may hold for a stored forward trajectory.
+constexpr size_t kAdjStoreDefault = (size_t)16 << 30;
 
 // Growable device allocation.
 struct DevBuf {
@@ -100,9 +102,25 @@ struct Batch {
     int last_adj_kind = kNone;
     JitKernel last_jit;
     std::string last_jit_error;
+    // Device memory the exact adjoint may hold for the whole forward
+    // trajectory ([nsteps+1][n][B]); within it the trajectory is written once
+    // by the forward kernel and read back, otherwise states are recomputed
+    // from checkpoints every ceil(sqrt(nsteps)) steps.  Same results either way.
+    size_t adj_store_limit = kAdjStoreDefault;
+    bool adj_stores(int n_sys, int nsteps) const {
+        return nsteps > 0 && (size_t)(nsteps + 1) * (size_t)plan->pat.n * (size_t)n_sys * rsize() <= adj_store_limit;
+    }
 
     bool f32() const { return plan->precision != kFP64; }
     size_t rsize() const { return f32() ? sizeof(float) : sizeof(double); }
+    // The specialised forward kernel for these reducers (false: none, *jerr why).
+    bool fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long long sm, bool with_traj, JitKernel* k,
+                    std::string* jerr);
+    // Launch it over [step0, step0 + nsteps) on state_p ([n][B], updated in
+    // place), trajectory slots into traj_p when traj_every > 0.
+    cudaError_t launch_fwd_jit(const JitKernel& k, const Signals& sig, double h, int step0, int nsteps,
+                               const Reducers& red, unsigned long long mm, unsigned long long sm, int traj_every,
+                               long long traj_slots, void* state_p, void* traj_p, cudaStream_t st);
 
     // New instance count; the device buffers are kept and grown by the next
     // set / solve when needed (a batch reused for requests of any size).

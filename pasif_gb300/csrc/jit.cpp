@@ -386,6 +386,9 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
              " int b) const {\n";
         for (int k = 0; k < MM; ++k) o << "    X[" << k << "] = src[" << own[k] << "LL * B + b];\n";
         o << "  }\n";
+        o << "  __device__ __forceinline__ void prefetch_vec(const R* src, long long B, int b) const {\n";
+        for (int k = 0; k < MM; ++k) o << "    pk_prefetch_l2(src + " << own[k] << "LL * B + b);\n";
+        o << "  }\n";
         o << "  template <class V> __device__ __forceinline__ void store_vec(const V& X, R* dst, long long B, int b)"
              " const {\n";
         for (int k = 0; k < MM; ++k) o << "    dst[" << own[k] << "LL * B + b] = X[" << k << "];\n";
@@ -834,18 +837,28 @@ bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey&
     return get_cached(fwd_source(pat, lit, key), "pk_fwd", key.block, out, err);
 }
 
-int ws_slices(const Pattern& pat, bool f32, bool force) {
+int ws_slices(const Pattern& pat, bool f32, bool force, int B) {
     const int n = pat.n;
-    // measured crossover on GB300: thread per system wins below ~28 states in FP32, ~24 in FP64
-    if (n < 2 || n > kWsMaxN || (!force && n < (f32 ? 28 : 24))) return 0;
+    // Measured crossovers on GB300 (time sliced / thread per system, 4096 systems):
+    // FP32 forward sliced from 28 states (16-state chain 1.34, 28 states 0.94).
+    // FP64 forward: its long dependent chains want more warps than one per
+    // system gives: 8-28 states 0.28-0.42; 4-5 states 0.47-0.59 for batches up
+    // to 8192 systems, 0.99 at 16384; 2 states 1.01.
+    if (n < 2 || n > kWsMaxN) return 0;
+    if (!force) {
+        const bool small_batch = B > 0 && B <= 8192;
+        if (f32 ? n < 28 : (n < 3 || (n < 8 && !small_batch))) return 0;
+    }
     return ws_split(n, f32, force, false);
 }
 
 int ws_slices_adjoint(const Pattern& pat, bool f32, bool force) {
     const int n = pat.n;
-    // the adjoint keeps about twice the vectors of the forward: sliced from 12 states
-    // (16-state chain: 2x the thread-per-system gradient rate, 236 -> 150 registers)
-    if (n < 2 || n > kWsMaxN || (!force && n < 12)) return 0;
+    // The adjoint keeps about twice the vectors of the forward.  Measured on
+    // GB300 (time sliced / thread per system, 1024-4096 systems): FP32 5
+    // states 0.75, 8 states 0.62, 4 states 0.93, 2 states 1.12; FP64 2 states
+    // 0.68, 4-8 states 0.33-0.44.
+    if (n < 2 || n > kWsMaxN || (!force && f32 && n < 5)) return 0;
     return ws_split(n, f32, force, true);
 }
 

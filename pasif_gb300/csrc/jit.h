@@ -39,9 +39,9 @@ struct JitKernel {
 };
 
 // Warps per 32 systems of the warp-sliced kernels for a pattern: 0 (thread
-// per system) below the size where the register-resident vectors spill,
-// unless `force`.
-int ws_slices(const Pattern& pat, bool f32, bool force);
+// per system) where that layout is faster (small systems in FP32), unless
+// `force`.  B: systems per launch (0: unknown, taken as large).
+int ws_slices(const Pattern& pat, bool f32, bool force, int B = 0);
 // Same for the exact adjoint (sliced from smaller systems).
 int ws_slices_adjoint(const Pattern& pat, bool f32, bool force);
 // Warps for n components (2..16).

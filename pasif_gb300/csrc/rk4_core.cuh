@@ -38,6 +38,26 @@ template <> struct M<float> {
     static __device__ __forceinline__ float max(float a, float b) { return fmaxf(a, b); }
 };
 
+// L2 prefetch of the line holding p (an address inside an allocation): the
+// backward sweep over a stored trajectory reads states written long before,
+// from HBM; prefetched kPrefetchSteps steps ahead they are in L2 when needed.
+constexpr int kPrefetchSteps = 8;
+
+// Trajectory slot of the state after `step` when every `every`-th state from
+// step0 is saved (-1: not saved); every == 1, the stored trajectory of the
+// adjoint, needs no division.
+__device__ __forceinline__ long long traj_slot(unsigned step, unsigned step0, int every) {
+    if (every == 1) return (long long)step - (long long)step0;
+    const unsigned e = (unsigned)every;
+    if (step % e != 0u) return -1;
+    return (long long)(step / e) - (long long)(step0 / e) - ((step0 % e) ? 1 : 0);
+}
+#ifndef PK_HOST_EMU
+__device__ __forceinline__ void pk_prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+#else
+static inline void pk_prefetch_l2(const void*) {}
+#endif
+
 // Register-resident vector (pattern-specialised kernels: every index is a
 // compile-time constant after unrolling).
 template <typename R, int N>
@@ -280,9 +300,8 @@ __device__ __forceinline__ void fwd_run(const Sys& sys, const FwdArgs<R>& a, int
         const R ub = force_at(a.frc, ebase, step, 0u, 1u);
         uc = force_at(a.frc, ebase, step, 1u, 0u);
         rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
-        if (HTRAJ && step % (unsigned)a.traj_every == 0u) {
-            const long long slot = (long long)(step / (unsigned)a.traj_every) - (long long)(a.step0 / (unsigned)a.traj_every)
-                                   - ((a.step0 % (unsigned)a.traj_every) ? 1 : 0);
+        if (HTRAJ) {
+            const long long slot = traj_slot(step, a.step0, a.traj_every);
             if (slot >= 0 && slot < a.traj_slots) {
 #pragma unroll
                 for (int i = 0; i < n; ++i) a.traj[(slot * n + i) * B + b] = Q[i];
@@ -360,10 +379,8 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     const long long ebase = rc.ebase;
     const unsigned len = frc.len;
     auto post = [&](unsigned step) {
-        if (HTRAJ && step % (unsigned)a.traj_every == 0u) {
-            const long long slot = (long long)(step / (unsigned)a.traj_every) -
-                                   (long long)(a.step0 / (unsigned)a.traj_every) -
-                                   ((a.step0 % (unsigned)a.traj_every) ? 1 : 0);
+        if (HTRAJ) {
+            const long long slot = traj_slot(step, a.step0, a.traj_every);
             if (slot >= 0 && slot < a.traj_slots) {
 #pragma unroll
                 for (int i = 0; i < N; ++i) a.traj[(slot * N + i) * B + b] = Q[i];
@@ -535,7 +552,7 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
 #pragma unroll
         for (int p = 0; p < P; ++p) pacc[p] = R(0);
     }
-    if (a.phase != 2) {   // forward pass with checkpoints
+    if (a.phase != 2 && !a.stored) {   // forward pass with checkpoints
         const int t0 = a.phase == 1 ? a.t_begin : 0, t1 = a.phase == 1 ? a.t_end : a.nsteps;
         if (t0 == 0) {
             for (int p = 0; p < P; ++p) PB[p] = 0.0;
@@ -571,6 +588,8 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
     RegVec<R, N> LAM, QN, CL;   // CL: compensation of LAM (Kahan mode)
     const int khi = a.phase == 2 ? a.k_hi : a.nck - 1, klo = a.phase == 2 ? a.k_lo : 0;
     if (khi == a.nck - 1) {
+        if (a.stored)   // no forward pass in this kernel zeroed the totals
+            for (int p = 0; p < P; ++p) PB[p] = 0.0;
 #pragma unroll
         for (int i = 0; i < N; ++i) { LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0); CL[i] = R(0); }
     } else {   // carried from the previous backward launch
@@ -581,25 +600,37 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
     for (int k = khi; k >= klo; --k) {
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
-        const R* ck = a.ckpt + (long long)k * 2 * N * B + b;
+        const int slot0 = a.stored ? 0 : start;   // buf slot of step t: t - slot0
+        if (!a.stored) {
+            const R* ck = a.ckpt + (long long)k * 2 * N * B + b;
 #pragma unroll
-        for (int i = 0; i < N; ++i) { Q[i] = ck[i * B]; Cm[i] = ck[(N + i) * B]; }
-        for (int t = start; t < end; ++t) {
-            R* bt = a.buf + (long long)(t - start) * N * B + b;
+            for (int i = 0; i < N; ++i) { Q[i] = ck[i * B]; Cm[i] = ck[(N + i) * B]; }
+            for (int t = start; t < end; ++t) {
+                R* bt = a.buf + (long long)(t - start) * N * B + b;
 #pragma unroll
-            for (int i = 0; i < N; ++i) bt[i * B] = Q[i];
-            const unsigned st = (unsigned)t;
-            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
-            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
-            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-            if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
-            else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+                for (int i = 0; i < N; ++i) bt[i * B] = Q[i];
+                const unsigned st = (unsigned)t;
+                const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+                const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+                const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+                if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+                else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+            }
+        } else {
+            const R* bt = a.buf + (long long)end * N * B + b;
+#pragma unroll
+            for (int i = 0; i < N; ++i) Q[i] = bt[i * B];
         }
 #pragma unroll
         for (int i = 0; i < N; ++i) QN[i] = Q[i];
         for (int t = end - 1; t >= start; --t) {
             RegVec<R, N> QC, Y2, Y3, Y4, QB, KB, YB;
-            const R* bt = a.buf + (long long)(t - start) * N * B + b;
+            if (a.stored && t >= kPrefetchSteps) {
+                const R* pf = a.buf + (long long)(t - kPrefetchSteps) * N * B + b;
+#pragma unroll
+                for (int i = 0; i < N; ++i) pk_prefetch_l2(pf + i * B);
+            }
+            const R* bt = a.buf + (long long)(t - slot0) * N * B + b;
 #pragma unroll
             for (int i = 0; i < N; ++i) QC[i] = bt[i * B];
             if (HSQ && a.g_sq && t >= a.sq_start) {
@@ -961,10 +992,8 @@ __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const
         }
         ws_step<R, KAHAN>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act);
         if (act) {
-            if (HTRAJ && out && step % (unsigned)a.traj_every == 0u) {
-                const long long slot = (long long)(step / (unsigned)a.traj_every) -
-                                       (long long)(a.step0 / (unsigned)a.traj_every) -
-                                       ((a.step0 % (unsigned)a.traj_every) ? 1 : 0);
+            if (HTRAJ && out) {
+                const long long slot = traj_slot(step, a.step0, a.traj_every);
                 if (slot >= 0 && slot < a.traj_slots) sl.store_traj(Q, a.traj + slot * N * B, B, b);
             }
             if (HMAX && (long long)step >= (long long)rc.max_start) sl.track_max(Q, Mx);
@@ -1084,7 +1113,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
 #pragma unroll
     for (int p = 0; p < (STEP_ACC ? PO : 1); ++p) pst[p] = R(0);
     V Q, Cm, S, K, Mi;
-    if (a.phase != 2) {   // forward pass with checkpoints (phase 1: steps [t_begin, t_end))
+    if (a.phase != 2 && !a.stored) {   // forward pass with checkpoints (phase 1: steps [t_begin, t_end))
         const int t0 = a.phase == 1 ? a.t_begin : 0, t1 = a.phase == 1 ? a.t_end : a.nsteps;
         if (t0 == 0) {
             if constexpr (STEP_ACC) {
@@ -1124,6 +1153,9 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     V LAM, QN, CL;   // CL: compensation of LAM (Kahan mode)
     const int khi = a.phase == 2 ? a.k_hi : a.nck - 1, klo = a.phase == 2 ? a.k_lo : 0;
     if (khi == a.nck - 1) {
+        if constexpr (STEP_ACC) {   // no forward pass in this kernel zeroed the totals
+            if (a.stored && valid) sl.zero_pbar(a.pbar, B, b);
+        }
         if (a.g_final) sl.load_vec(LAM, a.g_final, B, b);
         else {
 #pragma unroll
@@ -1144,25 +1176,32 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     for (int k = khi; k >= klo; --k) {
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
-        const R* ck = a.ckpt + (long long)k * 2 * N * B;
-        sl.load_vec(Q, ck, B, b);
-        sl.load_vec(Cm, ck + (long long)N * B, B, b);
-        sl.publish(Q, rq);
-        pk_block_sync();
-        for (int t = start; t < end; ++t) {
-            if (valid) sl.store_vec(Q, a.buf + (long long)(t - start) * N * B, B, b);
-            const unsigned st = (unsigned)t;
-            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
-            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
-            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-            ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
+        const int slot0 = a.stored ? 0 : start;   // buf slot of step t: t - slot0
+        if (!a.stored) {
+            const R* ck = a.ckpt + (long long)k * 2 * N * B;
+            sl.load_vec(Q, ck, B, b);
+            sl.load_vec(Cm, ck + (long long)N * B, B, b);
+            sl.publish(Q, rq);
+            pk_block_sync();
+            for (int t = start; t < end; ++t) {
+                if (valid) sl.store_vec(Q, a.buf + (long long)(t - start) * N * B, B, b);
+                const unsigned st = (unsigned)t;
+                const R ua = force_at(a.frc, ebase, st, 0u, 0u);
+                const R ub = force_at(a.frc, ebase, st, 0u, 1u);
+                const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+                ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
+            }
+        } else {
+            sl.load_vec(Q, a.buf + (long long)end * N * B, B, b);
         }
 #pragma unroll
         for (int i = 0; i < MM; ++i) QN[i] = Q[i];
         for (int t = end - 1; t >= start; --t) {
             V QC, Y2, Y3, Y4, QB, KB, YB;
-            // the chunk states were written by this thread (own components) before the barriers above
-            sl.load_vec(QC, a.buf + (long long)(t - start) * N * B, B, b);
+            if (a.stored && t >= kPrefetchSteps) sl.prefetch_vec(a.buf + (long long)(t - kPrefetchSteps) * N * B, B, b);
+            // the chunk states were written by this thread (own components) before the barriers above,
+            // or (stored) by an earlier kernel
+            sl.load_vec(QC, a.buf + (long long)(t - slot0) * N * B, B, b);
             if (HSQ && a.g_sq && t >= a.sq_start) sl.template add_sq_grad<KAHAN>(LAM, CL, QN, gsq2h);
             const unsigned st = (unsigned)t;
             const R ua = force_at(a.frc, ebase, st, 0u, 0u);

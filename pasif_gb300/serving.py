@@ -452,6 +452,7 @@ class Server:
                 plan = self._plans.setdefault(id(spec), plan)
         sig = Signals(req.signals, spec.window, spec.im, self.precision, stream=stream)
         b = Batch(plan, req.values, req.x0, req.exc_index, stream=stream)
+        b.adjoint_storage(0)   # checkpointed: the memory adjoint_bytes() books
         if self.reserve:   # grown buffers are fresh: upload the request again afterwards
             max_sys, max_steps, max_samples = self.reserve
             b.reserve(max_sys, max_steps)

@@ -276,6 +276,29 @@ int main(int argc, char** argv) {
     a.sq_start = sq_start;
     std::vector<R> lamc((size_t)B * n, R(0));
     a.lamc = lamc.data();
+    // EMU_ADJ_STORED=1: backward over a stored trajectory.  The states are
+    // made by this kernel's own forward pass with a checkpoint before every
+    // step (C = 1, one step past the horizon), copied to [nsteps+1][n][B].
+    const char* stored = std::getenv("EMU_ADJ_STORED");
+    std::vector<R> traj;
+    if (stored && std::atoi(stored) && nsteps > 0) {
+        std::vector<R> ck1((size_t)B * 2 * n * (nsteps + 1));
+        pk::AdjArgs<R> f = a;
+        f.ckpt = ck1.data();
+        f.C = 1;
+        f.nck = nsteps + 1;
+        f.nsteps = nsteps + 1;
+        f.phase = 1;
+        f.t_begin = 0;
+        f.t_end = nsteps + 1;
+        for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_adj(f); });
+        traj.assign((size_t)B * n * (nsteps + 1), R(0));
+        for (int t = 0; t <= nsteps; ++t)
+            for (size_t k = 0; k < (size_t)n * B; ++k) traj[(size_t)t * n * B + k] = ck1[(size_t)t * 2 * n * B + k];
+        a.buf = traj.data();
+        a.stored = 1;
+        std::fill(pbar.begin(), pbar.end(), -1.0);   // the stored backward must zero the totals itself
+    }
     // EMU_ADJ_SPLIT=k: the launch split of Batch::adjoint with k checkpoint
     // intervals per launch (forward segments, then backward chunk groups)
     const char* split = std::getenv("EMU_ADJ_SPLIT");
@@ -283,7 +306,7 @@ int main(int argc, char** argv) {
     if (per <= 0 || nck <= 2 * per) {
         for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_adj(a); });
     } else {
-        for (int t0 = 0; t0 < nsteps; t0 += per * C) {
+        for (int t0 = 0; t0 < (a.stored ? 0 : nsteps); t0 += per * C) {
             a.phase = 1;
             a.t_begin = t0;
             a.t_end = std::min(nsteps, t0 + per * C);

@@ -126,3 +126,28 @@ def test_adjoint_fp32_kahan_within_bound(gpu):
     assert np.median(err) <= 1e-6, np.median(err)
     assert err.max() <= 5e-5, err.max()
     np.testing.assert_array_equal(out[("fp32_kahan", False)][1], out[("fp32_kahan", True)][1])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
+@pytest.mark.parametrize("config,n_sys,nsteps,slicing", [
+    ("chain8", 40, 300, None),       # warp-sliced, one launch
+    ("chain8", 1024, 20_000, None),  # warp-sliced, split backward launches
+    ("duffing", 4096, 5_000, None),   # thread per system, split backward launches
+    ("chain8", 200, 997, False),     # thread per system, ragged last chunk
+])
+def test_adjoint_stored_equals_checkpointed(gpu, prec, config, n_sys, nsteps, slicing):
+    """The adjoint over a stored trajectory (the forward kernel writes every
+    state once) gives the bits of the checkpointed adjoint (checkpoint pass,
+    per-chunk recompute)."""
+    w = synth.CONFIGS[config](n_sys=n_sys, nsteps=nsteps)
+    rng = np.random.default_rng(77)
+    gf = rng.normal(size=(n_sys, w.pattern.n))
+    out = []
+    for storage in (0, 1 << 34):
+        b = Batch(Plan(w.pattern, prec, slicing=slicing), w.values, w.x0, w.exc_index)
+        b.adjoint_storage(storage)
+        out.append(b.adjoint(Signals(w.signals, w.window, w.im, prec), w.h, w.nsteps, g_final=gf,
+                             g_sq=np.ones(n_sys), sq_comp=(0,), sq_start=nsteps // 2))
+        assert b.kernel_info()["adjoint"] == "specialised"
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])

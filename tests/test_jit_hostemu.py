@@ -44,7 +44,8 @@ def build_emulator(d, src, define=None):
 
 def run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, h, step0, nsteps, prec, slicing=None):
     src = Plan(pat, prec, slicing=slicing).jit_report(vals, window=W, im=im).split("// ---- source ----\n", 1)[1]
-    assert ("warp-sliced" in src) == (bool(slicing) or (slicing is None and pat.n >= 28))
+    default_sliced = pat.n >= 28 if prec != "fp64" else pat.n >= 8 or (pat.n >= 3 and len(vals) <= 8192)
+    assert ("warp-sliced" in src) == (bool(slicing) or (slicing is None and default_sliced))
     d = str(tmp_path)
     exe, env = build_emulator(d, src)
     dt = np.float64 if prec == "fp64" else np.float32
@@ -79,9 +80,11 @@ def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps,
     np.testing.assert_array_equal(got, ref)
 
 
-def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, sq_start, h=0.03, split=0):
+def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, sq_start, h=0.03, split=0,
+                         stored=False):
     """split > 0: run it as the split launches of Batch::adjoint with `split`
-    checkpoint intervals per launch."""
+    checkpoint intervals per launch.  stored: backward sweep over a stored
+    trajectory (no checkpoint pass, no chunk recompute)."""
     mask = sum(1 << c for c in sq)
     src = Plan(pat, prec, slicing=slicing).jit_report_adjoint(vals, sq_mask=mask)
     src = src.split("// ---- source ----\n", 1)[1]
@@ -89,6 +92,8 @@ def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N,
     exe, env = build_emulator(d, src, "EMU_ADJ")
     if split:
         env["EMU_ADJ_SPLIT"] = str(split)
+    if stored:
+        env["EMU_ADJ_STORED"] = "1"
     dt = np.float64 if prec == "fp64" else np.float32
     B = len(vals)
     np.ascontiguousarray(vals.T, dt).tofile(os.path.join(d, "vals.bin"))
@@ -149,6 +154,24 @@ def test_generated_adjoint_fp32_sliced_equals_thread(tmp_path, seed):
         d = os.path.join(str(tmp_path), str(slicing))
         os.makedirs(d)
         out.append(run_emulated_adjoint(d, pat, "fp32_kahan", slicing, vals, x0, exc, x, im, gf, gs, N, sq, N // 3))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("split", [0, 2])
+@pytest.mark.parametrize("prec,slicing", [("fp64", False), ("fp64", True), ("fp32_kahan", False),
+                                          ("fp32_kahan", True)])
+def test_generated_adjoint_stored_equals_checkpointed(tmp_path, prec, slicing, split):
+    """The backward sweep over a stored trajectory (one forward pass) gives
+    the bits of the checkpointed adjoint (forward pass, then per-chunk
+    recompute), in one launch and as split backward launches."""
+    pat, vals, x0, exc, x, im, gf, gs, N, sq = _adjoint_case(1)
+    out = []
+    for stored in (False, True):
+        d = os.path.join(str(tmp_path), str(stored))
+        os.makedirs(d)
+        out.append(run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, N // 3,
+                                        split=split, stored=stored))
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
 

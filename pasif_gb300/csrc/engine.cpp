@@ -164,7 +164,8 @@ int Batch::reserve(int n_sys, int nsteps, std::string* err) {
     PK_CUDA(out_max.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(out_sq.ensure(Bn * rs), "cudaMalloc");
     PK_CUDA(ckpt.ensure(Bn * 2 * n * nck * rs), "cudaMalloc");
-    PK_CUDA(buf.ensure(Bn * n * (adj_stores((int)Bn, nsteps) ? (size_t)nsteps + 1 : C) * rs), "cudaMalloc");
+    PK_CUDA(buf.ensure(Bn * n * (adj_stores((int)Bn, nsteps) ? slot_vecs() * (size_t)nsteps + 1 : slot_vecs() * C) * rs),
+            "cudaMalloc");
     PK_CUDA(pbar.ensure(Bn * P * sizeof(double)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(gfin.ensure(Bn * n * rs), "cudaMalloc");
@@ -341,7 +342,7 @@ static int tps_block(int B) {
     return block;
 }
 
-bool Batch::fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long long sm, bool with_traj,
+bool Batch::fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long long sm, int traj_mode,
                        JitKernel* k, std::string* jerr) {
     const Pattern& pat = plan->pat;
     if (plan->generic_only || pat.n > kWsMaxN) {
@@ -354,7 +355,7 @@ bool Batch::fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long 
     key.kahan = plan->precision == kFP32Kahan;
     key.max_mask = mm;
     key.sq_mask = sm;
-    key.traj = with_traj;
+    key.traj = traj_mode;
     key.block = tps_block(B);
     key.window = (int)sig.w;
     key.wn.assign(sig.im_host.begin(), sig.im_host.begin() + sig.w);
@@ -410,7 +411,7 @@ int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Re
     const bool kahan = plan->precision == kFP32Kahan;
     JitKernel k;
     std::string jerr;
-    if (fwd_kernel(sig, mm, sm, traj_every > 0, &k, &jerr)) {
+    if (fwd_kernel(sig, mm, sm, traj_every > 0 ? 1 : 0, &k, &jerr)) {
         PK_CUDA(launch_fwd_jit(k, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots, state.p,
                                traj_every > 0 ? traj.p : nullptr, st),
                 "specialised forward kernel launch");
@@ -495,16 +496,17 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
                      get_adj_kernel(pat, lit, f, plan->precision == kFP32Kahan, g_sq ? sm : 0ull, slices, &jk, &jerr);
     if (!jit && !plan->generic_only) last_jit_error = jerr;
     // stored trajectory (specialised kernels, within adj_store_limit): the
-    // batch's forward kernel writes the state before every step once
+    // batch's forward kernel writes every step's slot once.  Otherwise a chunk
+    // of them ([C][slot_vecs][n][B]) is recomputed from checkpoints.
     JitKernel fk;
     std::string ferr;
-    const bool stored = jit && adj_stores(B, nsteps) && fwd_kernel(sig, 0ull, 0ull, true, &fk, &ferr);
+    const bool stored = jit && adj_stores(B, nsteps) && fwd_kernel(sig, 0ull, 0ull, 2, &fk, &ferr);
     const size_t vec = Bn * (size_t)n * rs;
     if (stored) {
-        PK_CUDA(buf.ensure((size_t)(nsteps + 1) * vec), "cudaMalloc");
+        PK_CUDA(buf.ensure((slot_vecs() * (size_t)nsteps + 1) * vec), "cudaMalloc");
     } else {
         PK_CUDA(ckpt.ensure(Bn * 2 * n * (size_t)(nck > 0 ? nck : 1) * rs), "cudaMalloc");
-        PK_CUDA(buf.ensure(Bn * (size_t)n * (size_t)C * rs), "cudaMalloc");
+        PK_CUDA(buf.ensure(slot_vecs() * (size_t)C * vec), "cudaMalloc");
     }
     PK_CUDA(pbar.ensure(Bn * (size_t)(P > 0 ? P : 1) * sizeof(double)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * (size_t)n * rs), "cudaMalloc");
@@ -516,11 +518,9 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
         int rc = upload_conv(g_sq, B, f, memory, gsq, adj_stage, st, err);
         if (rc) return rc;
     }
-    if (stored) {   // slot 0 = x0; slots 1..nsteps from the forward kernel (state in dx0, replaced later)
-        PK_CUDA(cudaMemcpyAsync(buf.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
+    if (stored) {   // the forward kernel's state runs in dx0 (replaced by the adjoint later)
         PK_CUDA(cudaMemcpyAsync(dx0.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
-        PK_CUDA(launch_fwd_jit(fk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, 1, nsteps, dx0.p,
-                               static_cast<char*>(buf.p) + vec, st),
+        PK_CUDA(launch_fwd_jit(fk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, 1, nsteps, dx0.p, buf.p, st),
                 "trajectory forward kernel launch");
     }
     cudaError_t e;

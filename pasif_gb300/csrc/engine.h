@@ -103,18 +103,22 @@ struct Batch {
     JitKernel last_jit;
     std::string last_jit_error;
     // Device memory the exact adjoint may hold for the whole forward
-    // trajectory ([nsteps+1][n][B]); within it the trajectory is written once
-    // by the forward kernel and read back, otherwise states are recomputed
-    // from checkpoints every ceil(sqrt(nsteps)) steps.  Same results either way.
+    // trajectory ([slot_vecs() nsteps + 1][n][B]: every step's state, FP64 also
+    // its stage inputs); within it the trajectory is written once by the
+    // forward kernel and read back, otherwise chunks of it are recomputed from
+    // checkpoints every ceil(sqrt(nsteps)) steps.  Same results either way.
     size_t adj_store_limit = kAdjStoreDefault;
+    size_t slot_vecs() const { return f32() ? 1 : 4; }   // adj_slot_vecs of rk4_core.cuh
     bool adj_stores(int n_sys, int nsteps) const {
-        return nsteps > 0 && (size_t)(nsteps + 1) * (size_t)plan->pat.n * (size_t)n_sys * rsize() <= adj_store_limit;
+        return nsteps > 0 && (slot_vecs() * (size_t)nsteps + 1) * (size_t)plan->pat.n * (size_t)n_sys * rsize() <=
+                                 adj_store_limit;
     }
 
     bool f32() const { return plan->precision != kFP64; }
     size_t rsize() const { return f32() ? sizeof(float) : sizeof(double); }
     // The specialised forward kernel for these reducers (false: none, *jerr why).
-    bool fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long long sm, bool with_traj, JitKernel* k,
+    // traj_mode: 0 none, 1 states every traj_every steps, 2 the adjoint trajectory.
+    bool fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long long sm, int traj_mode, JitKernel* k,
                     std::string* jerr);
     // Launch it over [step0, step0 + nsteps) on state_p ([n][B], updated in
     // place), trajectory slots into traj_p when traj_every > 0.

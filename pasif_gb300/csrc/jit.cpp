@@ -534,7 +534,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
     }
     o << "}  // namespace pk\n";
     const std::string kahan = key.kahan ? "true" : "false", hmax = key.max_mask ? "true" : "false",
-                      hsq = key.sq_mask ? "true" : "false", htraj = key.traj ? "true" : "false";
+                      hsq = key.sq_mask ? "true" : "false", htraj = std::to_string(key.traj);
     const char* sig = mode == 0 ? "pk_fwd(pk::FwdArgs<pk::R> a)" : mode == 1 ? "pk_pool(pk::PoolArgs<pk::R> p)"
                                                                             : "pk_adj(pk::AdjArgs<pk::R> a)";
     o << "extern \"C\" __global__ void __launch_bounds__(" << 32 * sl.L << ") " << sig << " {\n";
@@ -616,7 +616,7 @@ std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelK
     o << "  RegVec<R, " << n << "> Q, Cm, S, K, Mi, Mx;\n";
     o << "  fwd_run_iv<R, " << n << ", " << (key.kahan ? "true" : "false") << ", "
       << (key.max_mask ? "true" : "false") << ", " << (key.sq_mask ? "true" : "false") << ", "
-      << (key.traj ? "true" : "false") << ", JW>(sys, a, b, "
+      << key.traj << ", JW>(sys, a, b, "
       << key.max_mask << "ull, " << key.sq_mask << "ull, Q, Cm, S, K, Mi, Mx);\n";
     o << "}\n";
     return o.str();

@@ -22,7 +22,7 @@ struct FwdKernelKey {
     bool kahan = false;
     unsigned long long max_mask = 0;
     unsigned long long sq_mask = 0;
-    bool traj = false;
+    int traj = 0;                   // 1: states every traj_every steps; 2: adjoint trajectory (state + stage inputs)
     int block = 128;
     int window = 0;                 // forcing window (0 = sample and hold)
     std::vector<double> wn, wc;     // its weights in the compute precision

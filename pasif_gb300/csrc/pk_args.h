@@ -85,7 +85,9 @@ struct AdjArgs {
     const R* x0;                // [n][B]
     const int* exc_index;       // [B]
     R* ckpt;                    // [nck][2n][B] state + compensation at steps k*C
-    R* buf;                     // [C][n][B] recomputed chunk states, or (stored) [nsteps+1][n][B]
+    R* buf;                     // per step a slot: the state (FP64: and stage inputs Y2, Y3, Y4),
+                                // [adj_slot_vecs][n][B]; slots [C] of the recomputed chunk, or
+                                // (stored) [nsteps] + the final state (generic kernels: [C][n][B])
     R* scratch;                 // generic kernels: [16n][B]
     double* pbar;               // [P][B] parameter gradients (FP64 accumulation)
     R* dx0;                     // [n][B]
@@ -110,10 +112,10 @@ struct AdjArgs {
     int t_begin, t_end;
     int k_lo, k_hi;
     R* lamc;                    // [n][B] (Kahan mode)
-    // Stored trajectory: buf already holds the state before every step t
-    // (slot t, t = 0..nsteps), written by a forward kernel launched first, so
-    // there is no checkpoint pass and no chunk recompute; chunks only group
-    // the backward launches.
+    // Stored trajectory: buf already holds every step's slot t (t < nsteps)
+    // and the final state (state part of slot nsteps), written by a forward
+    // kernel launched first, so there is no checkpoint pass and no chunk
+    // recompute; chunks only group the backward launches.
     int stored;
 };
 

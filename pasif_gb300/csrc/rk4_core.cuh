@@ -52,6 +52,14 @@ __device__ __forceinline__ long long traj_slot(unsigned step, unsigned step0, in
     if (step % e != 0u) return -1;
     return (long long)(step / e) - (long long)(step0 / e) - ((step0 % e) ? 1 : 0);
 }
+
+// Vectors per step in a slot of an adjoint trajectory ([n][B] each): FP64
+// stores the state and the stage inputs Y2, Y3, Y4, so that the backward
+// sweep evaluates no right-hand side (FP64 arithmetic is its cost: 1.07 s ->
+// 0.88 s for 4096 16-state chains x 50000 steps on GB300); FP32 stores the
+// state only and recomputes the stages (moving four times the data cost more
+// than the arithmetic saved: 0.170 s -> 0.186 s on the same chains).
+template <typename R> __device__ __forceinline__ constexpr int adj_slot_vecs() { return sizeof(R) == 8 ? 4 : 1; }
 #ifndef PK_HOST_EMU
 __device__ __forceinline__ void pk_prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 #else
@@ -247,20 +255,39 @@ struct GenSys {
 // at u(step, half 1), k4 at u(step+1, half 0); Q += h/6 (k1 + 2k2 + 2k3 + k4)
 // with the sum formed as ((k1 + 2k2) + 2k3) + k4.  KAHAN: compensated update.
 // N > 0: compile-time size (registers); N == 0: runtime size sys.dim().
-template <typename R, int N, bool KAHAN, class Sys, class V>
+// NSTG = 1: the step's state is also stored to stg[i sB]; NSTG = 4: and its
+// stage inputs Y2, Y3, Y4 to stg[(j n + i) sB], j = 1..3: one slot of an
+// adjoint trajectory (adj_slot_vecs).
+template <typename R, int N, bool KAHAN, int NSTG = 0, class Sys, class V>
 __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K, V& Mi,
-                                         R ua, R ub, R uc, R h, R h2, R h6) {
+                                         R ua, R ub, R uc, R h, R h2, R h6, R* stg = nullptr, long long sB = 0) {
     typedef M<R> m;
     const int n = N ? N : sys.dim();
+    if constexpr (NSTG >= 1) {
+#pragma unroll
+        for (int i = 0; i < n; ++i) stg[i * sB] = Q[i];
+    }
     sys.template rhs<true>(Q, Q, ua, K);
 #pragma unroll
     for (int i = 0; i < n; ++i) { S[i] = K[i]; Mi[i] = m::fma(h2, K[i], Q[i]); }
+    if constexpr (NSTG == 4) {
+#pragma unroll
+        for (int i = 0; i < n; ++i) stg[(n + i) * sB] = Mi[i];
+    }
     sys.template rhs<true>(Mi, Mi, ub, K);
 #pragma unroll
     for (int i = 0; i < n; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(h2, K[i], Q[i]); }
+    if constexpr (NSTG == 4) {
+#pragma unroll
+        for (int i = 0; i < n; ++i) stg[(2 * n + i) * sB] = Mi[i];
+    }
     sys.template rhs<true>(Mi, Mi, ub, K);
 #pragma unroll
     for (int i = 0; i < n; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(h, K[i], Q[i]); }
+    if constexpr (NSTG == 4) {
+#pragma unroll
+        for (int i = 0; i < n; ++i) stg[(3 * n + i) * sB] = Mi[i];
+    }
     sys.template rhs<true>(Mi, Mi, uc, K);
 #pragma unroll
     for (int i = 0; i < n; ++i) {
@@ -367,7 +394,10 @@ struct RunCtx {
     int sq_start;
 };
 
-template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, class WP, class Sys, class V>
+// HTRAJ: 0 none; 1 the state after every traj_every-th step into a.traj
+// ([slot][N][B]); 2 the adjoint trajectory: before every step its slot into
+// a.traj ([step - step0][adj_slot_vecs][N][B], see rk4_step).
+template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, class WP, class Sys, class V>
 __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a, const Forcing<R>& frc, int b,
                                             const RunCtx& rc, unsigned long long max_mask,
                                             unsigned long long sq_mask, V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx,
@@ -375,11 +405,15 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     typedef M<R> m;
     constexpr int W = WP::W;
     constexpr unsigned SPI = W == 0 ? 1u : (unsigned)(W / 2);
+    constexpr int STG = HTRAJ == 2 ? adj_slot_vecs<R>() : 0;
     const long long B = a.B;
     const long long ebase = rc.ebase;
     const unsigned len = frc.len;
+    auto slot = [&](unsigned step) -> R* {
+        return STG ? a.traj + (long long)(step - a.step0) * STG * N * B + b : nullptr;
+    };
     auto post = [&](unsigned step) {
-        if (HTRAJ) {
+        if (HTRAJ == 1) {
             const long long slot = traj_slot(step, a.step0, a.traj_every);
             if (slot >= 0 && slot < a.traj_slots) {
 #pragma unroll
@@ -410,8 +444,9 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     unsigned s = rc.step0;
     const unsigned end = rc.step0 + rc.nsteps;
     while (s < end && (s % SPI) != 0u) {
-        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u), force_at(frc, ebase, s, 0u, 1u),
-                              force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6);
+        rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
+                                   force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6,
+                                   slot(s), B);
         post(s);
         ++s;
     }
@@ -437,7 +472,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
                     if (2 * r + 2 < W) un = g0 ? m::fma(WP::wc(2 * r + 2), x0, m::mul(WP::wn(2 * r + 2), x1)) : R(0);
                     else un = g1 ? m::fma(WP::wc(0), x1, m::mul(WP::wn(0), x2)) : R(0);
                 }
-                rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6);
+                rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6, slot(s + (unsigned)r), B);
                 post(s + (unsigned)r);
                 uc = un;
             }
@@ -447,16 +482,18 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
         }
     }
     while (s < end) {
-        rk4_step<R, N, KAHAN>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u), force_at(frc, ebase, s, 0u, 1u),
-                              force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6);
+        rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
+                                   force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6,
+                                   slot(s), B);
         post(s);
         ++s;
     }
 }
 
 // One batch instance over the whole horizon (initial state in a.state, final
-// state and reducers out).
-template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, class WP, class Sys, class V>
+// state and reducers out).  HTRAJ as fwd_core_iv; 2 also stores the final
+// state in slot nsteps (its state part).
+template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, class WP, class Sys, class V>
 __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, int b,
                                            unsigned long long max_mask, unsigned long long sq_mask,
                                            V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx) {
@@ -478,6 +515,10 @@ __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, 
                                                    sqc);
 #pragma unroll
     for (int i = 0; i < N; ++i) a.state[i * B + b] = Q[i];
+    if (HTRAJ == 2) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) a.traj[((long long)a.nsteps * adj_slot_vecs<R>() * N + i) * B + b] = Q[i];
+    }
     if (HMAX) {
         int slot = 0;
 #pragma unroll
@@ -522,7 +563,7 @@ __device__ __forceinline__ void pool_run_iv(const Sys& sys, const PoolArgs<R>& p
     rc.nsteps = (unsigned)(rem < p.chunk ? rem : p.chunk);
     rc.max_start = p.max_start[b];
     rc.sq_start = p.sq_start[b];
-    fwd_core_iv<R, N, KAHAN, HMAX, HSQ, false, WP>(sys, a, frc, b, rc, max_mask, sq_mask, Q, Cm, S, K, Mi, Mx, sq, sqc);
+    fwd_core_iv<R, N, KAHAN, HMAX, HSQ, 0, WP>(sys, a, frc, b, rc, max_mask, sq_mask, Q, Cm, S, K, Mi, Mx, sq, sqc);
 #pragma unroll
     for (int i = 0; i < N; ++i) {
         p.state[i * C + b] = Q[i];
@@ -547,6 +588,7 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
     const long long B = a.B;
     GVec<double> PB{a.pbar + b, B};
     const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
+    constexpr int SV = adj_slot_vecs<R>();
     RegVec<R, N> Q, Cm, S, K, Mi;
     if (STEP_ACC) {
 #pragma unroll
@@ -605,34 +647,63 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
             const R* ck = a.ckpt + (long long)k * 2 * N * B + b;
 #pragma unroll
             for (int i = 0; i < N; ++i) { Q[i] = ck[i * B]; Cm[i] = ck[(N + i) * B]; }
-            for (int t = start; t < end; ++t) {
-                R* bt = a.buf + (long long)(t - start) * N * B + b;
-#pragma unroll
-                for (int i = 0; i < N; ++i) bt[i * B] = Q[i];
+            for (int t = start; t < end; ++t) {   // slot: state (and FP64: stage inputs) of step t
+                R* bt = a.buf + (long long)(t - start) * SV * N * B + b;
                 const unsigned st = (unsigned)t;
                 const R ua = force_at(a.frc, ebase, st, 0u, 0u);
                 const R ub = force_at(a.frc, ebase, st, 0u, 1u);
                 const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-                if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
-                else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+                if (a.kahan) rk4_step<R, N, true, SV>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, bt, B);
+                else rk4_step<R, N, false, SV>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, bt, B);
             }
         } else {
-            const R* bt = a.buf + (long long)end * N * B + b;
+            const R* bt = a.buf + (long long)end * SV * N * B + b;
 #pragma unroll
             for (int i = 0; i < N; ++i) Q[i] = bt[i * B];
         }
 #pragma unroll
         for (int i = 0; i < N; ++i) QN[i] = Q[i];
+        // the step's state and stage inputs, as the forward computed them; small
+        // systems load the next step's slot one step ahead (latency hidden)
+        constexpr bool PIPE = SV == 4 && N <= 4;
+        RegVec<R, PIPE ? 4 * N : 1> nxt;
+        if constexpr (PIPE) {
+            const R* bt = a.buf + (long long)(end - 1 - slot0) * 4 * N * B + b;
+#pragma unroll
+            for (int i = 0; i < 4 * N; ++i) nxt[i] = bt[i * B];
+        }
         for (int t = end - 1; t >= start; --t) {
             RegVec<R, N> QC, Y2, Y3, Y4, QB, KB, YB;
             if (a.stored && t >= kPrefetchSteps) {
-                const R* pf = a.buf + (long long)(t - kPrefetchSteps) * N * B + b;
+                const R* pf = a.buf + (long long)(t - kPrefetchSteps) * SV * N * B + b;
 #pragma unroll
-                for (int i = 0; i < N; ++i) pk_prefetch_l2(pf + i * B);
+                for (int i = 0; i < SV * N; ++i) pk_prefetch_l2(pf + i * B);
             }
-            const R* bt = a.buf + (long long)(t - slot0) * N * B + b;
+            if constexpr (PIPE) {
 #pragma unroll
-            for (int i = 0; i < N; ++i) QC[i] = bt[i * B];
+                for (int i = 0; i < N; ++i) {
+                    QC[i] = nxt[i];
+                    Y2[i] = nxt[N + i];
+                    Y3[i] = nxt[2 * N + i];
+                    Y4[i] = nxt[3 * N + i];
+                }
+                if (t > start) {
+                    const R* bt = a.buf + (long long)(t - 1 - slot0) * 4 * N * B + b;
+#pragma unroll
+                    for (int i = 0; i < 4 * N; ++i) nxt[i] = bt[i * B];
+                }
+            } else {
+                const R* bt = a.buf + (long long)(t - slot0) * SV * N * B + b;
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                    QC[i] = bt[i * B];
+                    if constexpr (SV == 4) {
+                        Y2[i] = bt[(N + i) * B];
+                        Y3[i] = bt[(2 * N + i) * B];
+                        Y4[i] = bt[(3 * N + i) * B];
+                    }
+                }
+            }
             if (HSQ && a.g_sq && t >= a.sq_start) {
 #pragma unroll
                 for (int i = 0; i < N; ++i)
@@ -645,18 +716,21 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
             const R ua = force_at(a.frc, ebase, st, 0u, 0u);
             const R ub = force_at(a.frc, ebase, st, 0u, 1u);
             const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-            sys.template rhs<true>(QC, QC, ua, K);
+            if constexpr (SV == 1) {   // the stage inputs, recomputed
+                sys.template rhs<true>(QC, QC, ua, K);
 #pragma unroll
-            for (int i = 0; i < N; ++i) Y2[i] = m::fma(a.h2, K[i], QC[i]);
-            sys.template rhs<true>(Y2, Y2, ub, K);
+                for (int i = 0; i < N; ++i) Y2[i] = m::fma(a.h2, K[i], QC[i]);
+                sys.template rhs<true>(Y2, Y2, ub, K);
 #pragma unroll
-            for (int i = 0; i < N; ++i) Y3[i] = m::fma(a.h2, K[i], QC[i]);
-            sys.template rhs<true>(Y3, Y3, ub, K);
+                for (int i = 0; i < N; ++i) Y3[i] = m::fma(a.h2, K[i], QC[i]);
+                sys.template rhs<true>(Y3, Y3, ub, K);
+#pragma unroll
+                for (int i = 0; i < N; ++i) Y4[i] = m::fma(a.h, K[i], QC[i]);
+            }
             // QB sums the step's increment of LAM: onto LAM itself (plain), or
             // from 0 and then added with compensation (Kahan mode)
 #pragma unroll
             for (int i = 0; i < N; ++i) {
-                Y4[i] = m::fma(a.h, K[i], QC[i]);
                 KB[i] = m::mul(a.h6, LAM[i]);
                 QB[i] = a.kahan ? R(0) : LAM[i];
             }
@@ -928,13 +1002,21 @@ __device__ __forceinline__ unsigned pk_warp_max(unsigned v) { return __reduce_ma
 // code; with large slices the unrolled stages of the warps sharing an SM
 // sub-partition overflow its instruction cache (fetch stalls dominated), with
 // small slices the unrolled form is faster (fewer instructions).
-template <typename R, bool KAHAN, class SL, class V>
+//
+// NSTG: the slice's components of the state (1), and of the stage inputs Y2,
+// Y3, Y4 (4), are also stored to stg + j part ([N][B] each) when `store`: one
+// slot of an adjoint trajectory (as rk4_step).
+template <typename R, bool KAHAN, int NSTG = 0, class SL, class V>
 __device__ __forceinline__ void ws_step(const SL& sl, R* b0, R* b1, V& Q, V& Cm, V& S, V& K, V& Mi, R ua, R ub,
-                                        R uc, R h, R h2, R h6, bool act) {
+                                        R uc, R h, R h2, R h6, bool act, R* stg = nullptr, long long part = 0,
+                                        long long sB = 0, int b = 0, bool store = false) {
     typedef M<R> m;
     constexpr int MM = SL::MM;
 #pragma unroll
     for (int i = 0; i < MM; ++i) Mi[i] = Q[i];   // stage 1 evaluates at Q
+    if constexpr (NSTG >= 1) {
+        if (store) sl.store_vec(Q, stg, sB, b);
+    }
 #pragma unroll(SL::ROLL ? 1 : 4)
     for (int st = 0; st < 4; ++st) {
         const R u = st == 0 ? ua : (st == 3 ? uc : ub);
@@ -964,13 +1046,18 @@ __device__ __forceinline__ void ws_step(const SL& sl, R* b0, R* b1, V& Q, V& Cm,
 #pragma unroll
                 for (int i = 0; i < MM; ++i) { S[i] = m::fma(R(2), K[i], S[i]); Mi[i] = m::fma(c, K[i], Q[i]); }
             }
+            if constexpr (NSTG == 4) {
+                if (store) sl.store_vec(Mi, stg + (long long)(st + 1) * part, sB, b);
+            }
             sl.publish(Mi, (st & 1) ? b0 : b1);
         }
         pk_block_sync();
     }
 }
 
-template <typename R, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, int N, class SL, class V>
+// HTRAJ: as fwd_core_iv (1 states after every traj_every-th step, 2 the
+// adjoint trajectory).
+template <typename R, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, int N, class SL, class V>
 __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const Forcing<R>& frc, R* sm, int b,
                                         bool out, const RunCtx& rc, unsigned T, V& Q, V& Cm, V& Mx, R& sq,
                                         R& sqc) {
@@ -990,9 +1077,14 @@ __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const
             ub = force_at(frc, rc.ebase, step, 0u, 1u);
             uc = force_at(frc, rc.ebase, step, 1u, 0u);
         }
-        ws_step<R, KAHAN>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act);
+        if constexpr (HTRAJ == 2)
+            ws_step<R, KAHAN, adj_slot_vecs<R>()>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act,
+                                                  a.traj + (long long)(step - a.step0) * adj_slot_vecs<R>() * N * B,
+                                                  (long long)N * B, B, b, out && act);
+        else
+            ws_step<R, KAHAN>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act);
         if (act) {
-            if (HTRAJ && out) {
+            if (HTRAJ == 1 && out) {
                 const long long slot = traj_slot(step, a.step0, a.traj_every);
                 if (slot >= 0 && slot < a.traj_slots) sl.store_traj(Q, a.traj + slot * N * B, B, b);
             }
@@ -1005,7 +1097,7 @@ __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const
 // Batch forward (FwdArgs): lane b of every warp of the block; `valid` is false
 // for the lanes past the batch, which run a copy of the last system and store
 // nothing.
-template <typename R, bool KAHAN, bool HMAX, bool HSQ, bool HTRAJ, int N, class SL>
+template <typename R, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, int N, class SL>
 __device__ __forceinline__ void ws_fwd(SL& sl, const FwdArgs<R>& a, R* sm, int b, bool valid) {
     typedef RegVec<R, SL::MM> V;
     const long long B = a.B;
@@ -1024,6 +1116,7 @@ __device__ __forceinline__ void ws_fwd(SL& sl, const FwdArgs<R>& a, R* sm, int b
     ws_core<R, KAHAN, HMAX, HSQ, HTRAJ, N>(sl, a, a.frc, sm, b, valid, rc, (unsigned)a.nsteps, Q, Cm, Mx, sq, sqc);
     if (!valid) return;
     sl.store_vec(Q, a.state, B, b);
+    if (HTRAJ == 2) sl.store_vec(Q, a.traj + (long long)a.nsteps * adj_slot_vecs<R>() * N * B, B, b);
     if (HMAX) sl.store_max(Mx, a.out_max, B, b);
     if (HSQ && SL::SQOWN) a.out_sq[b] = sq;
 }
@@ -1070,7 +1163,7 @@ __device__ __forceinline__ void ws_pool(SL& sl, const PoolArgs<R>& p, R* sm, int
     rc.nsteps = mine;
     rc.max_start = p.max_start[b];
     rc.sq_start = p.sq_start[b];
-    ws_core<R, KAHAN, HMAX, HSQ, false, N>(sl, a, frc, sm, b, false, rc, T, Q, Cm, Mx, sq, sqc);
+    ws_core<R, KAHAN, HMAX, HSQ, 0, N>(sl, a, frc, sm, b, false, rc, T, Q, Cm, Mx, sq, sqc);
     if (mine == 0u) return;
     sl.store_vec(Q, p.state, C, b);
     if (KAHAN) sl.store_vec(Cm, p.comp, C, b);
@@ -1102,6 +1195,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     R* const r4 = sm + 3 * NP * 32;
     R* const k0 = sm + 4 * NP * 32;
     R* const k1 = sm + 5 * NP * 32;
+    constexpr int SV = adj_slot_vecs<R>();
     sl.load(a.vals, B, b);
     const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
     // FP64 totals: in registers (FP64 path), or in pbar itself when the FP32
@@ -1183,61 +1277,97 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             sl.load_vec(Cm, ck + (long long)N * B, B, b);
             sl.publish(Q, rq);
             pk_block_sync();
-            for (int t = start; t < end; ++t) {
-                if (valid) sl.store_vec(Q, a.buf + (long long)(t - start) * N * B, B, b);
+            for (int t = start; t < end; ++t) {   // slot: state (and FP64: stage inputs) of step t
                 const unsigned st = (unsigned)t;
                 const R ua = force_at(a.frc, ebase, st, 0u, 0u);
                 const R ub = force_at(a.frc, ebase, st, 0u, 1u);
                 const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-                ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
+                ws_step<R, KAHAN, SV>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true,
+                                      a.buf + (long long)(t - start) * SV * N * B, (long long)N * B, B, b, valid);
             }
         } else {
-            sl.load_vec(Q, a.buf + (long long)end * N * B, B, b);
+            sl.load_vec(Q, a.buf + (long long)end * SV * N * B, B, b);
         }
 #pragma unroll
         for (int i = 0; i < MM; ++i) QN[i] = Q[i];
+        // the step's slot as the forward computed it (own components: written by
+        // this thread before the barriers above, or by an earlier kernel).  FP64
+        // slots hold the stage inputs too, published to rq, r2, r3, r4 for the
+        // other slices; small slices load the next step's slot one step ahead.
+        constexpr bool PIPE = SV == 4 && MM <= 4;
+        auto load_slot = [&](int t, V& q, V& y2, V& y3, V& y4) {
+            const R* bt = a.buf + (long long)(t - slot0) * SV * N * B;
+            sl.load_vec(q, bt, B, b);
+            if constexpr (SV == 4) {
+                sl.load_vec(y2, bt + (long long)N * B, B, b);
+                sl.load_vec(y3, bt + 2LL * N * B, B, b);
+                sl.load_vec(y4, bt + 3LL * N * B, B, b);
+            }
+        };
+        V nQC, nY2, nY3, nY4;
+        if constexpr (PIPE) load_slot(end - 1, nQC, nY2, nY3, nY4);
         for (int t = end - 1; t >= start; --t) {
             V QC, Y2, Y3, Y4, QB, KB, YB;
-            if (a.stored && t >= kPrefetchSteps) sl.prefetch_vec(a.buf + (long long)(t - kPrefetchSteps) * N * B, B, b);
-            // the chunk states were written by this thread (own components) before the barriers above,
-            // or (stored) by an earlier kernel
-            sl.load_vec(QC, a.buf + (long long)(t - slot0) * N * B, B, b);
+            if (a.stored && t >= kPrefetchSteps) {
+                const R* pf = a.buf + (long long)(t - kPrefetchSteps) * SV * N * B;
+#pragma unroll
+                for (int j = 0; j < SV; ++j) sl.prefetch_vec(pf + (long long)j * N * B, B, b);
+            }
+            if constexpr (PIPE) {
+#pragma unroll
+                for (int i = 0; i < MM; ++i) { QC[i] = nQC[i]; Y2[i] = nY2[i]; Y3[i] = nY3[i]; Y4[i] = nY4[i]; }
+                if (t > start) load_slot(t - 1, nQC, nY2, nY3, nY4);
+            } else {
+                load_slot(t, QC, Y2, Y3, Y4);
+            }
             if (HSQ && a.g_sq && t >= a.sq_start) sl.template add_sq_grad<KAHAN>(LAM, CL, QN, gsq2h);
             const unsigned st = (unsigned)t;
             const R ua = force_at(a.frc, ebase, st, 0u, 0u);
             const R ub = force_at(a.frc, ebase, st, 0u, 1u);
             const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-            sl.publish(QC, rq);
-            pk_block_sync();
-            // stages: Y2 = QC + h/2 f(QC), Y3 = QC + h/2 f(Y2), Y4 = QC + h f(Y3), each
-            // published to its own region (rq, r2, r3, r4 follow each other); rolled
-            // like ws_step so that the right-hand side appears once in the code
+#pragma unroll
+            for (int i = 0; i < MM; ++i) {
+                KB[i] = m::mul(a.h6, LAM[i]);
+                QB[i] = KAHAN ? R(0) : LAM[i];   // the step's increment (Kahan) or LAM + it
+            }
             V Yc;
-#pragma unroll
-            for (int i = 0; i < MM; ++i) Yc[i] = QC[i];
-#pragma unroll(SL::ROLL ? 1 : 3)
-            for (int st = 0; st < 3; ++st) {
-                sl.rhs(Yc, rq + st * NP * 32, st == 0 ? ua : ub, K);
-                const R c = st == 2 ? a.h : a.h2;
-#pragma unroll
-                for (int i = 0; i < MM; ++i) Yc[i] = m::fma(c, K[i], QC[i]);
-                if (st == 0) {
-#pragma unroll
-                    for (int i = 0; i < MM; ++i) Y2[i] = Yc[i];
-                } else if (st == 1) {
-#pragma unroll
-                    for (int i = 0; i < MM; ++i) Y3[i] = Yc[i];
-                } else {
-#pragma unroll
-                    for (int i = 0; i < MM; ++i) {
-                        Y4[i] = Yc[i];
-                        KB[i] = m::mul(a.h6, LAM[i]);
-                        QB[i] = KAHAN ? R(0) : LAM[i];   // the step's increment (Kahan) or LAM + it
-                    }
-                    sl.publish(KB, k0);
-                }
-                sl.publish(Yc, rq + (st + 1) * NP * 32);
+            if constexpr (SV == 4) {
+                sl.publish(QC, rq);
+                sl.publish(Y2, r2);
+                sl.publish(Y3, r3);
+                sl.publish(Y4, r4);
+                sl.publish(KB, k0);
                 pk_block_sync();
+#pragma unroll
+                for (int i = 0; i < MM; ++i) Yc[i] = Y4[i];
+            } else {
+                // stages: Y2 = QC + h/2 f(QC), Y3 = QC + h/2 f(Y2), Y4 = QC + h f(Y3),
+                // each published to its own region (rq, r2, r3, r4 follow each
+                // other); rolled like ws_step so the right-hand side appears once
+                sl.publish(QC, rq);
+                sl.publish(KB, k0);
+                pk_block_sync();
+#pragma unroll
+                for (int i = 0; i < MM; ++i) Yc[i] = QC[i];
+#pragma unroll(SL::ROLL ? 1 : 3)
+                for (int st = 0; st < 3; ++st) {
+                    sl.rhs(Yc, rq + st * NP * 32, st == 0 ? ua : ub, K);
+                    const R c = st == 2 ? a.h : a.h2;
+#pragma unroll
+                    for (int i = 0; i < MM; ++i) Yc[i] = m::fma(c, K[i], QC[i]);
+                    if (st == 0) {
+#pragma unroll
+                        for (int i = 0; i < MM; ++i) Y2[i] = Yc[i];
+                    } else if (st == 1) {
+#pragma unroll
+                        for (int i = 0; i < MM; ++i) Y3[i] = Yc[i];
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < MM; ++i) Y4[i] = Yc[i];
+                    }
+                    sl.publish(Yc, rq + (st + 1) * NP * 32);
+                    pk_block_sync();
+                }
             }
             // reverse sweep: VJPs at Y4, Y3, Y2, QC with weights from k0, k1, k0, k1
 #pragma unroll(SL::ROLL ? 1 : 4)

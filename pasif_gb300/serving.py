@@ -173,13 +173,14 @@ class Result:
 def adjoint_bytes(pattern: Pattern, n_sys: int, nsteps: int, table: int, precision: str) -> int:
     """Device memory one adjoint request holds (the buffers pasif_batch_adjoint
     sizes: values, x0, state, checkpoints of state + compensation every
-    ceil(sqrt(N)) steps, the recomputed chunk, FP64 gradients, scratch of the
-    generic kernel, the signal table)."""
+    ceil(sqrt(N)) steps, the recomputed chunk of states (FP64: and stage
+    inputs), FP64 gradients, scratch of the generic kernel, the signal table)."""
     rs = 8 if precision == "fp64" else 4
     n, P = pattern.n, pattern.P
     c = max(1, math.ceil(math.sqrt(max(nsteps, 1))))
     nck = max(1, -(-nsteps // c))
-    per_sys = rs * (P + 3 * n + 2 * n * nck + c * n + 16 * n + 2) + 8 * (P + n)
+    sv = 4 if precision == "fp64" else 1
+    per_sys = rs * (P + 3 * n + 2 * n * nck + sv * c * n + 16 * n + 2) + 8 * (P + n)
     return int(n_sys * per_sys + rs * table + 4 * n_sys)
 
 

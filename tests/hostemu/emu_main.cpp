@@ -251,7 +251,7 @@ int main(int argc, char** argv) {
     auto gfin = readf<R>(dir, "gfin.bin", (size_t)n * B);
     const int C = nsteps > 0 ? (int)std::ceil(std::sqrt((double)nsteps)) : 1;
     const int nck = nsteps > 0 ? (nsteps + C - 1) / C : 0;
-    std::vector<R> ckpt((size_t)B * 2 * n * (nck > 0 ? nck : 1)), buf((size_t)B * n * C), dx0((size_t)B * n);
+    std::vector<R> ckpt((size_t)B * 2 * n * (nck > 0 ? nck : 1)), buf((size_t)B * 4 * n * C), dx0((size_t)B * n);
     std::vector<double> pbar((size_t)B * (P > 0 ? P : 1));
     pk::AdjArgs<R> a;
     std::memset(&a, 0, sizeof a);
@@ -276,25 +276,24 @@ int main(int argc, char** argv) {
     a.sq_start = sq_start;
     std::vector<R> lamc((size_t)B * n, R(0));
     a.lamc = lamc.data();
-    // EMU_ADJ_STORED=1: backward over a stored trajectory.  The states are
-    // made by this kernel's own forward pass with a checkpoint before every
-    // step (C = 1, one step past the horizon), copied to [nsteps+1][n][B].
+    // EMU_ADJ_STORED=1: backward over a stored trajectory ([nsteps+1][4][n][B]
+    // slots).  It is made by this kernel's own chunk recompute: the adjoint of
+    // one step more, in one chunk, leaves slots 0..nsteps in its buffer.
     const char* stored = std::getenv("EMU_ADJ_STORED");
-    std::vector<R> traj;
+    std::vector<R> traj, ck1((size_t)B * 2 * n), dx1((size_t)B * n), lc1((size_t)B * n, R(0));
+    std::vector<double> pb1(pbar.size());
     if (stored && std::atoi(stored) && nsteps > 0) {
-        std::vector<R> ck1((size_t)B * 2 * n * (nsteps + 1));
+        traj.assign((size_t)B * 4 * n * (nsteps + 1), R(0));
         pk::AdjArgs<R> f = a;
         f.ckpt = ck1.data();
-        f.C = 1;
-        f.nck = nsteps + 1;
+        f.buf = traj.data();
+        f.pbar = pb1.data();
+        f.dx0 = dx1.data();
+        f.lamc = lc1.data();
+        f.C = nsteps + 1;
+        f.nck = 1;
         f.nsteps = nsteps + 1;
-        f.phase = 1;
-        f.t_begin = 0;
-        f.t_end = nsteps + 1;
         for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_adj(f); });
-        traj.assign((size_t)B * n * (nsteps + 1), R(0));
-        for (int t = 0; t <= nsteps; ++t)
-            for (size_t k = 0; k < (size_t)n * B; ++k) traj[(size_t)t * n * B + k] = ck1[(size_t)t * 2 * n * B + k];
         a.buf = traj.data();
         a.stored = 1;
         std::fill(pbar.begin(), pbar.end(), -1.0);   // the stored backward must zero the totals itself

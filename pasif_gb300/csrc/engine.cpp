@@ -164,8 +164,11 @@ int Batch::reserve(int n_sys, int nsteps, std::string* err) {
     PK_CUDA(out_max.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(out_sq.ensure(Bn * rs), "cudaMalloc");
     PK_CUDA(ckpt.ensure(Bn * 2 * n * nck * rs), "cudaMalloc");
-    PK_CUDA(buf.ensure(Bn * n * (adj_stores((int)Bn, nsteps) ? slot_vecs() * (size_t)nsteps + 1 : slot_vecs() * C) * rs),
-            "cudaMalloc");
+    // the recomputed chunk, or the largest stored trajectory a request up to
+    // this size may use (within adj_store_limit)
+    const size_t chunk_bytes = Bn * n * slot_vecs() * C * rs;
+    const size_t full_bytes = Bn * n * (slot_vecs() * (size_t)nsteps + 1) * rs;
+    PK_CUDA(buf.ensure(std::max(chunk_bytes, nsteps > 0 ? std::min(full_bytes, adj_store_limit) : 0)), "cudaMalloc");
     PK_CUDA(pbar.ensure(Bn * P * sizeof(double)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(gfin.ensure(Bn * n * rs), "cudaMalloc");

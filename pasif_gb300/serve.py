@@ -23,7 +23,8 @@ from . import synth
 
 
 def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, capacity=16384,
-        arena_samples=1 << 25, adjoint_budget=48 << 30, adjoint_workers=None, check=6, log=None) -> dict:
+        arena_samples=1 << 25, adjoint_budget=96 << 30, adjoint_workers=None, adjoint_storage=3 << 30, check=6,
+        log=None) -> dict:
     dofs = tuple(dofs or synth.SERVED_DOFS)
     specs = S.served_specs(dofs)
     stream = synth.served_stream(rate, duration, seed, dofs=dofs)
@@ -33,7 +34,7 @@ def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, cap
     if adjoint_workers is None:   # more workers where one adjoint is long and uses few SMs
         adjoint_workers = {d: 6 if s.pattern.n >= 60 else 4 if s.pattern.n >= 24 else 2 for d, s in specs.items()}
     srv = S.Server(specs, precision, capacity, arena_samples, adjoint_budget, adjoint_workers,
-                   reserve=(4096, 200_000, 4 * 200_003))
+                   reserve=(4096, 200_000, 4 * 200_003), adjoint_storage=adjoint_storage)
     t = time.perf_counter()
     srv.warm()
     t_warm = time.perf_counter() - t
@@ -61,6 +62,9 @@ def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, cap
         "requests_per_s": len(ok) / out["wall_s"],
         "precision": precision, "chunk_launches": {str(k): v for k, v in sorted(chunks.items())},
         "kernels_ready_s": round(t_warm, 1),
+        "adjoint_memory": {"budget_bytes": int(adjoint_budget), "stored_trajectory_bytes_per_worker": int(adjoint_storage),
+                           "workers": {str(k): v for k, v in sorted(adjoint_workers.items())}
+                           if isinstance(adjoint_workers, dict) else adjoint_workers},
         "errors": sorted({x.error for x in res.values() if x.error})[:5],
         "by_dof": {str(d): {kind: {"n": len(v), "p50_ms": round(S.percentile(v, 50), 1),
                                    "p99_ms": round(S.percentile(v, 99), 1)}
@@ -116,10 +120,12 @@ def main():
     ap.add_argument("--precision", default="fp32_kahan")
     ap.add_argument("--dofs", type=str, default="")
     ap.add_argument("--check", type=int, default=6)
+    ap.add_argument("--adjoint-storage", type=float, default=3.0,
+                    help="GiB per adjoint worker for stored forward trajectories (0: always checkpointed)")
     a = ap.parse_args()
     dofs = tuple(int(x) for x in a.dofs.split(",")) if a.dofs else None
     print(json.dumps(run(a.rate, a.duration, a.seed, a.precision, dofs, check=a.check,
-                         log=lambda m: print(m, flush=True))))
+                         adjoint_storage=int(a.adjoint_storage * (1 << 30)), log=lambda m: print(m, flush=True))))
 
 
 if __name__ == "__main__":

@@ -170,17 +170,24 @@ class Result:
         return self.t_done - self.t_arrival
 
 
-def adjoint_bytes(pattern: Pattern, n_sys: int, nsteps: int, table: int, precision: str) -> int:
+def adjoint_bytes(pattern: Pattern, n_sys: int, nsteps: int, table: int, precision: str, storage: int = 0) -> int:
     """Device memory one adjoint request holds (the buffers pasif_batch_adjoint
-    sizes: values, x0, state, checkpoints of state + compensation every
-    ceil(sqrt(N)) steps, the recomputed chunk of states (FP64: and stage
-    inputs), FP64 gradients, scratch of the generic kernel, the signal table)."""
+    sizes: values, x0, state, FP64 gradients, scratch of the generic kernel,
+    the signal table, and either the stored trajectory, when it fits in
+    `storage` bytes (Batch.adjoint_storage), or checkpoints of state +
+    compensation every ceil(sqrt(N)) steps and the recomputed chunk).  A
+    trajectory slot is the state, and in FP64 also the stage inputs."""
     rs = 8 if precision == "fp64" else 4
     n, P = pattern.n, pattern.P
-    c = max(1, math.ceil(math.sqrt(max(nsteps, 1))))
-    nck = max(1, -(-nsteps // c))
     sv = 4 if precision == "fp64" else 1
-    per_sys = rs * (P + 3 * n + 2 * n * nck + sv * c * n + 16 * n + 2) + 8 * (P + n)
+    full = (sv * nsteps + 1) * n
+    if nsteps > 0 and n_sys * full * rs <= storage:
+        traj = full
+    else:
+        c = max(1, math.ceil(math.sqrt(max(nsteps, 1))))
+        nck = max(1, -(-nsteps // c))
+        traj = 2 * n * nck + sv * c * n
+    per_sys = rs * (P + 3 * n + traj + 16 * n + 2) + 8 * (P + n)
     return int(n_sys * per_sys + rs * table + 4 * n_sys)
 
 
@@ -198,12 +205,16 @@ class Server:
     def __init__(self, specs: dict, precision: str = "fp32_kahan", capacity: int = 8192,
                  arena_samples: int = 1 << 24, adjoint_budget: int = 8 << 30, adjoint_workers: int = 2,
                  pool_factory=None, adjoint_runner=None, stream_factory=None, clock=time.perf_counter,
-                 reserve=None):
+                 reserve=None, adjoint_storage: int = 0):
         """reserve = (max systems, max steps, max signal samples) of an adjoint
         request: each worker sizes its batch and signal table for it on its
-        first request, so later ones allocate nothing."""
+        first request, so later ones allocate nothing.  adjoint_storage:
+        device bytes per adjoint worker batch for stored forward trajectories
+        (a request whose trajectory fits skips the checkpoint recompute, about
+        one forward pass; 0: always checkpointed)."""
         self.specs = dict(specs)
         self.reserve = reserve
+        self.adjoint_storage = int(adjoint_storage)
         self.precision = precision
         self.capacity = int(capacity)
         self.arena_samples = int(arena_samples)
@@ -320,7 +331,7 @@ class Server:
                 self._cv.notify_all()
         elif req.kind == "adjoint":
             spec = self.specs[req.cls]
-            need = adjoint_bytes(spec.pattern, req.n_sys, req.nsteps, table, self.precision)
+            need = adjoint_bytes(spec.pattern, req.n_sys, req.nsteps, table, self.precision, self.adjoint_storage)
             if need > self.adjoint_budget:
                 return self._finish(res, error=f"adjoint needs {need} bytes, budget {self.adjoint_budget}")
             with self._cv:
@@ -453,7 +464,7 @@ class Server:
                 plan = self._plans.setdefault(id(spec), plan)
         sig = Signals(req.signals, spec.window, spec.im, self.precision, stream=stream)
         b = Batch(plan, req.values, req.x0, req.exc_index, stream=stream)
-        b.adjoint_storage(0)   # checkpointed: the memory adjoint_bytes() books
+        b.adjoint_storage(self.adjoint_storage)   # the memory adjoint_bytes() books
         if self.reserve:   # grown buffers are fresh: upload the request again afterwards
             max_sys, max_steps, max_samples = self.reserve
             b.reserve(max_sys, max_steps)

@@ -193,3 +193,17 @@ def test_served_stream_shape():
     frac = sum(r.kind == "adjoint" for r in st) / len(st)
     assert 0.2 < frac < 0.4
     assert {r.dof for r in st} == set(synth.SERVED_DOFS)
+
+
+def test_adjoint_bytes_stored_or_checkpointed():
+    """A request whose forward trajectory fits the per-worker storage books
+    the trajectory instead of checkpoints and the recomputed chunk; FP64
+    slots hold the stage inputs too."""
+    n, N, B = PAT.n, 1000, 8
+    ck = S.adjoint_bytes(PAT, B, N, 10, "fp32_kahan")
+    full = B * (N + 1) * n * 4
+    st = S.adjoint_bytes(PAT, B, N, 10, "fp32_kahan", storage=full)
+    assert st - ck == full - B * 4 * (2 * n * 32 + 32 * n)   # ceil(sqrt(1000)) = 32 steps per chunk, 32 chunks
+    assert S.adjoint_bytes(PAT, B, N, 10, "fp32_kahan", storage=full - 1) == ck
+    full64 = B * (4 * N + 1) * n * 8
+    assert S.adjoint_bytes(PAT, B, N, 10, "fp64", storage=full64) > S.adjoint_bytes(PAT, B, N, 10, "fp64")

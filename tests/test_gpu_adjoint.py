@@ -151,3 +151,13 @@ def test_adjoint_stored_equals_checkpointed(gpu, prec, config, n_sys, nsteps, sl
         assert b.kernel_info()["adjoint"] == "specialised"
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+def test_adjoint_storage_limit_validated(gpu):
+    w = synth.chain8(n_sys=4, nsteps=10)
+    b = Batch(Plan(w.pattern, "fp32_kahan"), w.values, w.x0, w.exc_index)
+    from pasif_gb300 import _native as N
+    with pytest.raises(N.PasifError) as e:
+        b.adjoint_storage(-1)
+    assert e.value.code == N.ERR_INVALID
+    b.adjoint_storage(0)

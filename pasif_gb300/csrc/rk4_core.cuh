@@ -629,14 +629,24 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
     }
     RegVec<R, N> LAM, QN, CL;   // CL: compensation of LAM (Kahan mode)
     const int khi = a.phase == 2 ? a.k_hi : a.nck - 1, klo = a.phase == 2 ? a.k_lo : 0;
+    // FP32 with few values: the FP64 totals in registers through the backward
+    // launch (the same additions as into pbar, in the same order)
+    constexpr bool PBREG = STEP_ACC && P <= 24;
+    RegVec<double, PBREG ? P : 1> PR;
+#pragma unroll
+    for (int p = 0; p < (PBREG ? P : 1); ++p) PR[p] = 0.0;
     if (khi == a.nck - 1) {
-        if (a.stored)   // no forward pass in this kernel zeroed the totals
+        if (a.stored && !PBREG)   // no forward pass in this kernel zeroed the totals
             for (int p = 0; p < P; ++p) PB[p] = 0.0;
 #pragma unroll
         for (int i = 0; i < N; ++i) { LAM[i] = a.g_final ? a.g_final[i * B + b] : R(0); CL[i] = R(0); }
     } else {   // carried from the previous backward launch
 #pragma unroll
         for (int i = 0; i < N; ++i) { LAM[i] = a.dx0[i * B + b]; CL[i] = a.kahan ? a.lamc[i * B + b] : R(0); }
+        if constexpr (PBREG) {
+#pragma unroll
+            for (int p = 0; p < P; ++p) PR[p] = PB[p];
+        }
     }
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
     for (int k = khi; k >= klo; --k) {
@@ -665,12 +675,12 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
         for (int i = 0; i < N; ++i) QN[i] = Q[i];
         // the step's state and stage inputs, as the forward computed them; small
         // systems load the next step's slot one step ahead (latency hidden)
-        constexpr bool PIPE = SV == 4 && N <= 4;
-        RegVec<R, PIPE ? 4 * N : 1> nxt;
+        constexpr bool PIPE = SV * N <= 16;
+        RegVec<R, PIPE ? SV * N : 1> nxt;
         if constexpr (PIPE) {
-            const R* bt = a.buf + (long long)(end - 1 - slot0) * 4 * N * B + b;
+            const R* bt = a.buf + (long long)(end - 1 - slot0) * SV * N * B + b;
 #pragma unroll
-            for (int i = 0; i < 4 * N; ++i) nxt[i] = bt[i * B];
+            for (int i = 0; i < SV * N; ++i) nxt[i] = bt[i * B];
         }
         for (int t = end - 1; t >= start; --t) {
             RegVec<R, N> QC, Y2, Y3, Y4, QB, KB, YB;
@@ -683,14 +693,16 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
 #pragma unroll
                 for (int i = 0; i < N; ++i) {
                     QC[i] = nxt[i];
-                    Y2[i] = nxt[N + i];
-                    Y3[i] = nxt[2 * N + i];
-                    Y4[i] = nxt[3 * N + i];
+                    if constexpr (SV == 4) {
+                        Y2[i] = nxt[N + i];
+                        Y3[i] = nxt[2 * N + i];
+                        Y4[i] = nxt[3 * N + i];
+                    }
                 }
                 if (t > start) {
-                    const R* bt = a.buf + (long long)(t - 1 - slot0) * 4 * N * B + b;
+                    const R* bt = a.buf + (long long)(t - 1 - slot0) * SV * N * B + b;
 #pragma unroll
-                    for (int i = 0; i < 4 * N; ++i) nxt[i] = bt[i * B];
+                    for (int i = 0; i < SV * N; ++i) nxt[i] = bt[i * B];
                 }
             } else {
                 const R* bt = a.buf + (long long)(t - slot0) * SV * N * B + b;
@@ -762,11 +774,18 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
                 else LAM[i] = m::add(QB[i], YB[i]);
                 QN[i] = QC[i];
             }
-            if (STEP_ACC) {
+            if constexpr (PBREG) {
+#pragma unroll
+                for (int p = 0; p < P; ++p) { PR[p] = PR[p] + (double)pacc[p]; pacc[p] = R(0); }
+            } else if (STEP_ACC) {
 #pragma unroll
                 for (int p = 0; p < P; ++p) { PB[p] = PB[p] + (double)pacc[p]; pacc[p] = R(0); }
             }
         }
+    }
+    if constexpr (PBREG) {
+#pragma unroll
+        for (int p = 0; p < P; ++p) PB[p] = PR[p];
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -1198,12 +1217,14 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     constexpr int SV = adj_slot_vecs<R>();
     sl.load(a.vals, B, b);
     const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
-    // FP64 totals: in registers (FP64 path), or in pbar itself when the FP32
-    // per-step sums (pst) are added once per step (keeps registers for the vectors)
-    RegVec<double, STEP_ACC ? 1 : PO> PB;
+    // FP64 totals in registers (FP64 path; FP32 with few values per slice), or
+    // in pbar itself, the FP32 per-step sums (pst) added once per step (keeps
+    // registers for the vectors).  Same additions in the same order either way.
+    constexpr bool PBREG = !STEP_ACC || PO <= 16;
+    RegVec<double, PBREG ? PO : 1> PB;
     RegVec<R, STEP_ACC ? PO : 1> pst;
 #pragma unroll
-    for (int p = 0; p < (STEP_ACC ? 1 : PO); ++p) PB[p] = 0.0;
+    for (int p = 0; p < (PBREG ? PO : 1); ++p) PB[p] = 0.0;
 #pragma unroll
     for (int p = 0; p < (STEP_ACC ? PO : 1); ++p) pst[p] = R(0);
     V Q, Cm, S, K, Mi;
@@ -1264,7 +1285,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
 #pragma unroll
             for (int i = 0; i < MM; ++i) CL[i] = R(0);
         }
-        if constexpr (!STEP_ACC) sl.load_pbar(PB, a.pbar, B, b);
+        if constexpr (PBREG) sl.load_pbar(PB, a.pbar, B, b);
     }
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
     for (int k = khi; k >= klo; --k) {
@@ -1294,7 +1315,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
         // this thread before the barriers above, or by an earlier kernel).  FP64
         // slots hold the stage inputs too, published to rq, r2, r3, r4 for the
         // other slices; small slices load the next step's slot one step ahead.
-        constexpr bool PIPE = SV == 4 && MM <= 4;
+        constexpr bool PIPE = SV == 1 || MM <= 4;
         auto load_slot = [&](int t, V& q, V& y2, V& y3, V& y4) {
             const R* bt = a.buf + (long long)(t - slot0) * SV * N * B;
             sl.load_vec(q, bt, B, b);
@@ -1315,7 +1336,10 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             }
             if constexpr (PIPE) {
 #pragma unroll
-                for (int i = 0; i < MM; ++i) { QC[i] = nQC[i]; Y2[i] = nY2[i]; Y3[i] = nY3[i]; Y4[i] = nY4[i]; }
+                for (int i = 0; i < MM; ++i) {
+                    QC[i] = nQC[i];
+                    if constexpr (SV == 4) { Y2[i] = nY2[i]; Y3[i] = nY3[i]; Y4[i] = nY4[i]; }
+                }
                 if (t > start) load_slot(t - 1, nQC, nY2, nY3, nY4);
             } else {
                 load_slot(t, QC, Y2, Y3, Y4);
@@ -1404,7 +1428,12 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                 QN[i] = QC[i];
             }
             if constexpr (STEP_ACC) {
-                if (valid) sl.add_pbar(pst, a.pbar, B, b);
+                if constexpr (PBREG) {
+#pragma unroll
+                    for (int p = 0; p < PO; ++p) PB[p] = PB[p] + (double)pst[p];
+                } else {
+                    if (valid) sl.add_pbar(pst, a.pbar, B, b);
+                }
 #pragma unroll
                 for (int p = 0; p < PO; ++p) pst[p] = R(0);
             }
@@ -1414,7 +1443,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     if (!valid) return;
     sl.store_vec(LAM, a.dx0, B, b);
     if (KAHAN && a.phase == 2) sl.store_vec(CL, a.lamc, B, b);
-    if constexpr (!STEP_ACC) sl.store_pbar(PB, a.pbar, B, b);
+    if constexpr (PBREG) sl.store_pbar(PB, a.pbar, B, b);
 }
 
 }  // namespace pk

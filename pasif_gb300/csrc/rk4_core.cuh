@@ -675,6 +675,9 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
         for (int i = 0; i < N; ++i) QN[i] = Q[i];
         // the step's state and stage inputs, as the forward computed them; small
         // systems load the next step's slot one step ahead (latency hidden)
+        R fa = force_at(a.frc, ebase, (unsigned)(end - 1), 0u, 0u);
+        R fb = force_at(a.frc, ebase, (unsigned)(end - 1), 0u, 1u);
+        R fc = force_at(a.frc, ebase, (unsigned)(end - 1), 1u, 0u);
         constexpr bool PIPE = SV * N <= 16;
         RegVec<R, PIPE ? SV * N : 1> nxt;
         if constexpr (PIPE) {
@@ -724,10 +727,13 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
                         else LAM[i] = m::fma(gsq2h, QN[i], LAM[i]);
                     }
             }
-            const unsigned st = (unsigned)t;
-            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
-            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
-            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            // the forcing of step t, read one step ahead (uc of step t-1 is ua of step t)
+            const R ua = fa, ub = fb, uc = fc;
+            if (t > start) {
+                fc = fa;
+                fa = force_at(a.frc, ebase, (unsigned)(t - 1), 0u, 0u);
+                fb = force_at(a.frc, ebase, (unsigned)(t - 1), 0u, 1u);
+            }
             if constexpr (SV == 1) {   // the stage inputs, recomputed
                 sys.template rhs<true>(QC, QC, ua, K);
 #pragma unroll
@@ -1327,6 +1333,9 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
         };
         V nQC, nY2, nY3, nY4;
         if constexpr (PIPE) load_slot(end - 1, nQC, nY2, nY3, nY4);
+        R fa = force_at(a.frc, ebase, (unsigned)(end - 1), 0u, 0u);
+        R fb = force_at(a.frc, ebase, (unsigned)(end - 1), 0u, 1u);
+        R fc = force_at(a.frc, ebase, (unsigned)(end - 1), 1u, 0u);
         for (int t = end - 1; t >= start; --t) {
             V QC, Y2, Y3, Y4, QB, KB, YB;
             if (a.stored && t >= kPrefetchSteps) {
@@ -1345,10 +1354,13 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                 load_slot(t, QC, Y2, Y3, Y4);
             }
             if (HSQ && a.g_sq && t >= a.sq_start) sl.template add_sq_grad<KAHAN>(LAM, CL, QN, gsq2h);
-            const unsigned st = (unsigned)t;
-            const R ua = force_at(a.frc, ebase, st, 0u, 0u);
-            const R ub = force_at(a.frc, ebase, st, 0u, 1u);
-            const R uc = force_at(a.frc, ebase, st, 1u, 0u);
+            // the forcing of step t, read one step ahead (uc of step t-1 is ua of step t)
+            const R ua = fa, ub = fb, uc = fc;
+            if (t > start) {
+                fc = fa;
+                fa = force_at(a.frc, ebase, (unsigned)(t - 1), 0u, 0u);
+                fb = force_at(a.frc, ebase, (unsigned)(t - 1), 0u, 1u);
+            }
 #pragma unroll
             for (int i = 0; i < MM; ++i) {
                 KB[i] = m::mul(a.h6, LAM[i]);

@@ -1092,15 +1092,21 @@ __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const
     V S, K, Mi;
     sl.publish(Q, b0);
     pk_block_sync();
-    R uc = SL::FORCED ? force_at(frc, rc.ebase, rc.step0, 0u, 0u) : R(0);
+    // the forcing of step s is read during step s - 1 (its ua is the uc before)
+    R na = R(0), nb = R(0), nc = R(0);
+    if (SL::FORCED) {
+        na = force_at(frc, rc.ebase, rc.step0, 0u, 0u);
+        nb = force_at(frc, rc.ebase, rc.step0, 0u, 1u);
+        nc = force_at(frc, rc.ebase, rc.step0, 1u, 0u);
+    }
     for (unsigned s = 0; s < T; ++s) {
         const bool act = s < rc.nsteps;
         const unsigned step = rc.step0 + s;
-        const R ua = uc;
-        R ub = R(0);
-        if (SL::FORCED) {
-            ub = force_at(frc, rc.ebase, step, 0u, 1u);
-            uc = force_at(frc, rc.ebase, step, 1u, 0u);
+        const R ua = na, ub = nb, uc = nc;
+        if (SL::FORCED && s + 1 < T) {
+            na = nc;
+            nb = force_at(frc, rc.ebase, step + 1u, 0u, 1u);
+            nc = force_at(frc, rc.ebase, step + 1u, 1u, 0u);
         }
         if constexpr (HTRAJ == 2)
             ws_step<R, KAHAN, adj_slot_vecs<R>()>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act,

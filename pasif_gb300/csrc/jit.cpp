@@ -573,6 +573,26 @@ void ws_launch(const std::string& src, int* block, int* smem) {
 
 }  // namespace
 
+// The thread's shared-memory ring of upcoming excitation samples (JW::ring):
+// with one or two steps per sample interval (W <= 4) and a short step, a
+// sample read one interval ahead leaves every step waiting for memory, so
+// samples are copied asynchronously (cp.async) RING - 1 intervals before they
+// are used.  Measured on GB300: 1024 one-DOF systems (86 FLOP per step, one
+// sample per step from a 410 MB table) 3.5e9 -> 1.5e10 system-steps/s; 4096
+// 16-state chains (644 FLOP per step), whose steps already cover the read,
+// 9.2e9 -> 3.9e9, so longer steps keep the register read-ahead.
+static void emit_sample_ring(std::ostringstream& o, int W, int block, const Pattern& pat) {
+    const int spi = W == 0 ? 1 : W / 2;
+    const long long flops = 4LL * (2 * pat.k_nnz() + 3 * pat.g_nnz() + 4 * pat.l_nnz() + 5 * pat.p_nnz() +
+                                   2 * pat.f_nnz() + 3) + 13LL * pat.n;
+    const int ring = spi <= 2 && flops <= 200 ? 16 : 0;
+    o << "  static constexpr int RING = " << ring << ", RS = " << block << ";\n";
+    if (ring)
+        o << "  __device__ static R* ring() { __shared__ R r[" << ring * block << "]; return r + threadIdx.x; }\n";
+    else
+        o << "  __device__ static R* ring() { return nullptr; }\n";
+}
+
 std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key) {
     if (key.slices >= 2) return ws_source(pat, lit, key, 0);
     Emitter em(pat, lit);
@@ -601,6 +621,7 @@ std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelK
     // forcing window and weights as compile-time constants
     const int W = key.window;
     o << "struct JW {\n  static constexpr int W = " << W << ";\n";
+    emit_sample_ring(o, W, key.block, pat);
     for (int which = 0; which < 2; ++which) {
         o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";
         const std::vector<double>& wv = which ? key.wc : key.wn;
@@ -791,6 +812,7 @@ std::string pool_source(const Pattern& pat, const FwdKernelKey& key) {
     o << "};\n";
     const int W = key.window;
     o << "struct JW {\n  static constexpr int W = " << W << ";\n";
+    emit_sample_ring(o, W, key.block, pat);
     for (int which = 0; which < 2; ++which) {
         o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";
         const std::vector<double>& wv = which ? key.wc : key.wn;

@@ -372,6 +372,32 @@ __device__ __forceinline__ R sample_at(const Forcing<R>& f, long long idx) {
     return idx < f.total ? f.x[idx] : R(0);
 }
 
+// Asynchronous copy of sample_at(f, idx) into shared memory (cp.async; past
+// the table's end the source size is 0 and the slot is zero-filled), and its
+// group commit / wait.
+#ifndef PK_HOST_EMU
+template <typename R>
+__device__ __forceinline__ void sample_async(R* dst, const Forcing<R>& f, long long idx) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const bool ok = idx < f.total;
+    const R* src = f.x + (ok ? idx : 0);
+    const int n = ok ? (int)sizeof(R) : 0;
+    if (sizeof(R) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory"); }
+#else
+template <typename R>
+static inline void sample_async(R* dst, const Forcing<R>& f, long long idx) { *dst = sample_at(f, idx); }
+static inline void async_commit() {}
+template <int PENDING>
+static inline void async_wait() {}
+#endif
+
 // Forward integration walking the excitation one sample interval at a time
 // (pattern-specialised kernels).  WP::W is the interpolation window (0 =
 // sample and hold) and WP::wn(i) / WP::wc(i) its next / current-sample
@@ -453,8 +479,28 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     if (end - s >= SPI) {
         unsigned j = s / SPI;
         R x0 = sample_at(frc, ebase + j), x1 = sample_at(frc, ebase + j + 1), x2 = sample_at(frc, ebase + j + 2);
+        // WP::RING > 0: sample j + 3 is copied into this thread's shared-memory
+        // ring (slot (j + 3) % RING, stride RS) RING - 1 intervals before use
+        constexpr int RING = WP::RING;
+        R* const ring = WP::ring();
+        if constexpr (RING > 0) {
+#pragma unroll
+            for (int q = 0; q < RING - 1; ++q) {
+                sample_async(ring + ((j + 3u + (unsigned)q) % (unsigned)RING) * WP::RS, frc, ebase + j + 3 + q);
+                async_commit();
+            }
+        }
         for (; end - s >= SPI; s += SPI, ++j) {
-            const R nxt = sample_at(frc, ebase + j + 3);
+            R nxt;
+            if constexpr (RING > 0) {
+                async_wait<RING - 2>();   // the copy of sample j + 3 (the oldest of RING - 1) has landed
+                nxt = ring[((j + 3u) % (unsigned)RING) * WP::RS];
+                // refill the slot read in the previous interval
+                sample_async(ring + ((j + 3u + RING - 1u) % (unsigned)RING) * WP::RS, frc, ebase + j + 3 + RING - 1);
+                async_commit();
+            } else {
+                nxt = sample_at(frc, ebase + j + 3);
+            }
             const bool g0 = j > 0u && j < len;
             const bool g1 = j + 1u > 0u && j + 1u < len;
             R uc;
@@ -480,6 +526,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
             x1 = x2;
             x2 = nxt;
         }
+        if constexpr (RING > 0) async_wait<0>();   // no copy outlives the loop
     }
     while (s < end) {
         rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),

@@ -20,6 +20,7 @@
 #define __noinline__
 #define __restrict__
 #define __launch_bounds__(x)
+#define __shared__ static
 static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
 static inline double __dmul_rn(double a, double b) { return a * b; }
 static inline double __dadd_rn(double a, double b) { return a + b; }

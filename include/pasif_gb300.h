@@ -205,11 +205,13 @@ int pasif_batch_resize(pasif_batch* b, int n_sys);
  * allocate nothing (cudaMalloc/cudaFree synchronise the device). */
 int pasif_batch_reserve(pasif_batch* b, int n_sys, int nsteps);
 /* Device memory (bytes) the exact adjoint may hold for the whole forward
- * trajectory, (nsteps + 1) * n * n_sys states.  Within it the forward
- * kernel writes every state once and the backward sweep reads them; above it
- * states are recomputed from checkpoints every ceil(sqrt(nsteps)) steps
- * (about one more forward pass).  Results are identical.  Default 16 GiB;
- * 0 always recomputes.  Set it before pasif_batch_reserve. */
+ * trajectory: (nsteps + 1) * n * n_sys FP32 states, or in FP64 every step's
+ * state and three stage inputs, (4 nsteps + 1) * n * n_sys doubles.  Within
+ * it the forward kernel writes the trajectory once and the backward sweep
+ * reads it; above it the trajectory is recomputed chunk by chunk from
+ * checkpoints every ceil(sqrt(nsteps)) steps (about one more forward pass).
+ * Results are identical.  Default 16 GiB; 0 always recomputes.  Set it
+ * before pasif_batch_reserve. */
 int pasif_batch_set_adjoint_storage(pasif_batch* b, long long bytes);
 /* values[n_sys][P], x0[n_sys][n], exc_index[n_sys]. */
 int pasif_batch_set(pasif_batch* b, const double* values, const double* x0, const int* exc_index,

@@ -166,7 +166,8 @@ int Batch::reserve(int n_sys, int nsteps, std::string* err) {
     PK_CUDA(ckpt.ensure(Bn * 2 * n * nck * rs), "cudaMalloc");
     // the recomputed chunk, or the largest stored trajectory a request up to
     // this size may use (within adj_store_limit)
-    const size_t chunk_bytes = Bn * n * slot_vecs() * C * rs;
+    const size_t chunk_bytes = Bn * n * (slot_vecs() * C + 1) * rs;
+    PK_CUDA(adj_state.ensure(Bn * n * rs), "cudaMalloc");
     const size_t full_bytes = Bn * n * (slot_vecs() * (size_t)nsteps + 1) * rs;
     PK_CUDA(buf.ensure(std::max(chunk_bytes, nsteps > 0 ? std::min(full_bytes, adj_store_limit) : 0)), "cudaMalloc");
     PK_CUDA(pbar.ensure(Bn * P * sizeof(double)), "cudaMalloc");
@@ -369,13 +370,15 @@ bool Batch::fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long 
 
 cudaError_t Batch::launch_fwd_jit(const JitKernel& k, const Signals& sig, double h, int step0, int nsteps,
                                   const Reducers& red, unsigned long long mm, unsigned long long sm, int traj_every,
-                                  long long traj_slots, void* state_p, void* traj_p, cudaStream_t st) {
+                                  long long traj_slots, void* state_p, void* traj_p, cudaStream_t st,
+                                  const void* comp_p) {
     const dim3 grid((unsigned)((B + k.per_block - 1) / k.per_block));
     if (f32()) {
         pk::FwdArgs<float> a;
         fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
         a.state = static_cast<float*>(state_p);
         a.traj = static_cast<float*>(traj_p);
+        a.comp = static_cast<const float*>(comp_p);
         void* args[] = {&a};
         return cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
     }
@@ -383,6 +386,7 @@ cudaError_t Batch::launch_fwd_jit(const JitKernel& k, const Signals& sig, double
     fill_fwd(a, *this, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots);
     a.state = static_cast<double*>(state_p);
     a.traj = static_cast<double*>(traj_p);
+    a.comp = static_cast<const double*>(comp_p);
     void* args[] = {&a};
     return cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
 }
@@ -498,19 +502,28 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     const bool jit = !plan->generic_only &&
                      get_adj_kernel(pat, lit, f, plan->precision == kFP32Kahan, g_sq ? sm : 0ull, slices, &jk, &jerr);
     if (!jit && !plan->generic_only) last_jit_error = jerr;
-    // stored trajectory (specialised kernels, within adj_store_limit): the
-    // batch's forward kernel writes every step's slot once.  Otherwise a chunk
-    // of them ([C][slot_vecs][n][B]) is recomputed from checkpoints.
-    JitKernel fk;
+    // The trajectory the backward sweep reads, in one of three ways (same bits):
+    //  stored   (within adj_store_limit): the batch's forward kernel writes
+    //           every step's slot once;
+    //  replayed (specialised forward kernel available): the forward kernel
+    //           writes checkpoints every C steps, then, chunk by chunk in
+    //           backward order, the chunk's slots from its checkpoint, each
+    //           followed by the adjoint kernel's backward sweep over them;
+    //  otherwise the adjoint kernel does the checkpoint pass and the chunk
+    //           recomputes itself (in its own warp layout).
+    JitKernel fk, ckk;
     std::string ferr;
     const bool stored = jit && adj_stores(B, nsteps) && fwd_kernel(sig, 0ull, 0ull, 2, &fk, &ferr);
+    const bool replayed = !stored && jit && nsteps > 0 && fwd_kernel(sig, 0ull, 0ull, 2, &fk, &ferr) &&
+                          fwd_kernel(sig, 0ull, 0ull, 3, &ckk, &ferr);
     const size_t vec = Bn * (size_t)n * rs;
     if (stored) {
         PK_CUDA(buf.ensure((slot_vecs() * (size_t)nsteps + 1) * vec), "cudaMalloc");
     } else {
         PK_CUDA(ckpt.ensure(Bn * 2 * n * (size_t)(nck > 0 ? nck : 1) * rs), "cudaMalloc");
-        PK_CUDA(buf.ensure(slot_vecs() * (size_t)C * vec), "cudaMalloc");
+        PK_CUDA(buf.ensure((slot_vecs() * (size_t)C + 1) * vec), "cudaMalloc");
     }
+    if (replayed) PK_CUDA(adj_state.ensure(vec), "cudaMalloc");
     PK_CUDA(pbar.ensure(Bn * (size_t)(P > 0 ? P : 1) * sizeof(double)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     if (g_final) {
@@ -525,6 +538,11 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
         PK_CUDA(cudaMemcpyAsync(dx0.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
         PK_CUDA(launch_fwd_jit(fk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, 1, nsteps, dx0.p, buf.p, st),
                 "trajectory forward kernel launch");
+    }
+    if (replayed) {   // checkpoints of state and compensation every C steps
+        PK_CUDA(cudaMemcpyAsync(adj_state.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
+        PK_CUDA(launch_fwd_jit(ckk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, C, nck, adj_state.p, ckpt.p, st),
+                "checkpoint forward kernel launch");
     }
     cudaError_t e;
 #define PK_FILL_ADJ(R_)                                               \
@@ -552,7 +570,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     a.kahan = plan->precision == kFP32Kahan ? 1 : 0;                  \
     a.sq_start = red.sq_start;                                        \
     a.sq_mask = g_sq ? sm : 0ull;                                     \
-    a.stored = stored ? 1 : 0;
+    a.stored = stored || replayed ? 1 : 0;
     const dim3 grid((unsigned)(jit ? (B + jk.per_block - 1) / jk.per_block : (B + 127) / 128));
     if (jit && plan->precision == kFP32Kahan) PK_CUDA(lamc.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     // Specialised kernels over many blocks: forward segments and backward chunk
@@ -564,8 +582,28 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     auto launch_jit = [&](auto& a) -> cudaError_t {
         void* args[] = {&a};
         a.lamc = lamc.as<typename std::remove_pointer<decltype(a.dx0)>::type>();
-        const int steps = std::max(1, kAdjLaunchSteps * 16 / std::max(16, n));
-        const int per = std::max(1, steps / C);   // checkpoint intervals per launch
+        // Replayed: per chunk, backward order, its slots from its checkpoint then
+        // its backward sweep; one chunk at a time keeps the slots in L2 between
+        // the two (groups of chunks, 2016 steps for 16 states, ran 3 % slower).
+        if (replayed) {
+            const size_t rsz = sizeof(*a.dx0);
+            for (int k = nck - 1; k >= 0; --k) {
+                const int t0 = k * C, t1 = std::min(nsteps, t0 + C);
+                const char* ck = static_cast<const char*>(ckpt.p) + (size_t)k * 2 * n * Bn * rsz;
+                cudaError_t le = cudaMemcpyAsync(adj_state.p, ck, vec, cudaMemcpyDeviceToDevice, st);
+                if (le != cudaSuccess) return le;
+                le = launch_fwd_jit(fk, sig, h, t0, t1 - t0, Reducers(), 0ull, 0ull, 1, t1 - t0, adj_state.p, buf.p,
+                                    st, ck + (size_t)n * Bn * rsz);
+                if (le != cudaSuccess) return le;
+                a.phase = 2;
+                a.k_hi = a.k_lo = k;
+                a.slot_base = t0;
+                le = cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
+                if (le != cudaSuccess) return le;
+            }
+            return cudaSuccess;
+        }
+        const int per = adj_group(n, C, nck);   // checkpoint intervals per launch
         if (nck <= 2 * per || grid.x < 32) {
             a.phase = 0;
             return cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);

@@ -21,6 +21,13 @@ enum KernelKind { kNone = 0, kGeneric = 1, kSpecialised = 2 };
 constexpr int kAdjLaunchSteps = 2048;
 // Default device memory an exact adjoint may hold for a stored forward trajectory.
 constexpr size_t kAdjStoreDefault = (size_t)16 << 30;
+// Checkpoint intervals (of C steps) per launch of a split exact adjoint:
+// about kAdjLaunchSteps * 16 / n steps, at most the nck intervals there are.
+inline int adj_group(int n, int C, int nck) {
+    const int steps = kAdjLaunchSteps * 16 / (n > 16 ? n : 16);
+    const int g = steps / (C > 0 ? C : 1) > 1 ? steps / (C > 0 ? C : 1) : 1;
+    return g < nck ? g : (nck > 1 ? nck : 1);
+}
 
 // Growable device allocation.
 struct DevBuf {
@@ -91,7 +98,7 @@ struct Batch {
     std::shared_ptr<Plan> plan;
     int B = 0;
     DevBuf vals, x0, state, exc, out_max, out_sq, scratch, stage, traj;
-    DevBuf ckpt, buf, pbar, dx0, gfin, gsq, adj_stage, lamc;
+    DevBuf ckpt, buf, pbar, dx0, gfin, gsq, adj_stage, lamc, adj_state;
     Literals lit;
     int n_max = 0;
     bool has_sq = false;
@@ -121,10 +128,12 @@ struct Batch {
     bool fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long long sm, int traj_mode, JitKernel* k,
                     std::string* jerr);
     // Launch it over [step0, step0 + nsteps) on state_p ([n][B], updated in
-    // place), trajectory slots into traj_p when traj_every > 0.
+    // place), trajectory slots (or checkpoints) into traj_p when traj_every >
+    // 0, starting from the Kahan compensation comp_p ([n][B]; null: zero).
     cudaError_t launch_fwd_jit(const JitKernel& k, const Signals& sig, double h, int step0, int nsteps,
                                const Reducers& red, unsigned long long mm, unsigned long long sm, int traj_every,
-                               long long traj_slots, void* state_p, void* traj_p, cudaStream_t st);
+                               long long traj_slots, void* state_p, void* traj_p, cudaStream_t st,
+                               const void* comp_p = nullptr);
 
     // New instance count; the device buffers are kept and grown by the next
     // set / solve when needed (a batch reused for requests of any size).

@@ -53,6 +53,11 @@ struct FwdArgs {
     int sq_start;
     unsigned long long max_mask;   // components reduced by max |q|
     unsigned long long sq_mask;    // components reduced by sum q^2
+    // Restart (pattern-specialised kernels): the initial Kahan compensation
+    // [n][B], or null for zero.  With trajectory mode 3 (checkpoints) the
+    // kernels store the state and compensation before every step t with
+    // t % traj_every == 0 to traj + (t / traj_every) [2n][B].
+    const R* comp;
 };
 
 // Serving pool: C slots of one pattern, each slot an instance of some request
@@ -112,11 +117,13 @@ struct AdjArgs {
     int t_begin, t_end;
     int k_lo, k_hi;
     R* lamc;                    // [n][B] (Kahan mode)
-    // Stored trajectory: buf already holds every step's slot t (t < nsteps)
-    // and the final state (state part of slot nsteps), written by a forward
-    // kernel launched first, so there is no checkpoint pass and no chunk
-    // recompute; chunks only group the backward launches.
+    // Stored trajectory: buf already holds the slots of steps slot_base ..
+    // (slot t - slot_base) and the state after the last of them (state part of
+    // the next slot), written by a forward kernel launched first, so there is
+    // no checkpoint pass and no chunk recompute in this kernel; chunks only
+    // group the backward launches.  slot_base = 0: the whole trajectory.
     int stored;
+    int slot_base;
 };
 
 // __GpuDriver::_getGradient semantics (see the oracle for the quirk list).

@@ -422,7 +422,9 @@ struct RunCtx {
 
 // HTRAJ: 0 none; 1 the state after every traj_every-th step into a.traj
 // ([slot][N][B]); 2 the adjoint trajectory: before every step its slot into
-// a.traj ([step - step0][adj_slot_vecs][N][B], see rk4_step).
+// a.traj ([step - step0][adj_slot_vecs][N][B], see rk4_step); 3 checkpoints
+// for the adjoint: the state and compensation before every traj_every-th
+// step into a.traj ([step / traj_every][2N][B]).
 template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, class WP, class Sys, class V>
 __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a, const Forcing<R>& frc, int b,
                                             const RunCtx& rc, unsigned long long max_mask,
@@ -437,6 +439,20 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     const unsigned len = frc.len;
     auto slot = [&](unsigned step) -> R* {
         return STG ? a.traj + (long long)(step - a.step0) * STG * N * B + b : nullptr;
+    };
+    // HTRAJ == 3: checkpoints, the state and compensation before every
+    // traj_every-th step
+    auto pre = [&](unsigned step) {
+        if constexpr (HTRAJ == 3) {
+            if (step % (unsigned)a.traj_every == 0u) {
+                R* ck = a.traj + (long long)(step / (unsigned)a.traj_every) * 2 * N * B + b;
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                    ck[i * B] = Q[i];
+                    ck[(N + i) * B] = KAHAN ? Cm[i] : R(0);
+                }
+            }
+        }
     };
     auto post = [&](unsigned step) {
         if (HTRAJ == 1) {
@@ -470,6 +486,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     unsigned s = rc.step0;
     const unsigned end = rc.step0 + rc.nsteps;
     while (s < end && (s % SPI) != 0u) {
+        pre(s);
         rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
                                    force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6,
                                    slot(s), B);
@@ -518,6 +535,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
                     if (2 * r + 2 < W) un = g0 ? m::fma(WP::wc(2 * r + 2), x0, m::mul(WP::wn(2 * r + 2), x1)) : R(0);
                     else un = g1 ? m::fma(WP::wc(0), x1, m::mul(WP::wn(0), x2)) : R(0);
                 }
+                pre(s + (unsigned)r);
                 rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6, slot(s + (unsigned)r), B);
                 post(s + (unsigned)r);
                 uc = un;
@@ -529,6 +547,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
         if constexpr (RING > 0) async_wait<0>();   // no copy outlives the loop
     }
     while (s < end) {
+        pre(s);
         rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
                                    force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6,
                                    slot(s), B);
@@ -548,7 +567,7 @@ __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, 
 #pragma unroll
     for (int i = 0; i < N; ++i) {
         Q[i] = a.state[i * B + b];
-        if (KAHAN) Cm[i] = R(0);
+        if (KAHAN) Cm[i] = a.comp ? a.comp[i * B + b] : R(0);
         if (HMAX) Mx[i] = R(0);
     }
     R sq = R(0), sqc = R(0);
@@ -699,7 +718,7 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
     for (int k = khi; k >= klo; --k) {
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
-        const int slot0 = a.stored ? 0 : start;   // buf slot of step t: t - slot0
+        const int slot0 = a.stored ? a.slot_base : start;   // buf slot of step t: t - slot0
         if (!a.stored) {
             const R* ck = a.ckpt + (long long)k * 2 * N * B + b;
 #pragma unroll
@@ -714,7 +733,7 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
                 else rk4_step<R, N, false, SV>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, bt, B);
             }
         } else {
-            const R* bt = a.buf + (long long)end * SV * N * B + b;
+            const R* bt = a.buf + (long long)(end - slot0) * SV * N * B + b;
 #pragma unroll
             for (int i = 0; i < N; ++i) Q[i] = bt[i * B];
         }
@@ -734,8 +753,8 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
         }
         for (int t = end - 1; t >= start; --t) {
             RegVec<R, N> QC, Y2, Y3, Y4, QB, KB, YB;
-            if (a.stored && t >= kPrefetchSteps) {
-                const R* pf = a.buf + (long long)(t - kPrefetchSteps) * SV * N * B + b;
+            if (a.stored && t - kPrefetchSteps >= slot0) {
+                const R* pf = a.buf + (long long)(t - kPrefetchSteps - slot0) * SV * N * B + b;
 #pragma unroll
                 for (int i = 0; i < SV * N; ++i) pk_prefetch_l2(pf + i * B);
             }
@@ -1128,7 +1147,7 @@ __device__ __forceinline__ void ws_step(const SL& sl, R* b0, R* b1, V& Q, V& Cm,
 }
 
 // HTRAJ: as fwd_core_iv (1 states after every traj_every-th step, 2 the
-// adjoint trajectory).
+// adjoint trajectory, 3 checkpoints).
 template <typename R, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, int N, class SL, class V>
 __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const Forcing<R>& frc, R* sm, int b,
                                         bool out, const RunCtx& rc, unsigned T, V& Q, V& Cm, V& Mx, R& sq,
@@ -1154,6 +1173,13 @@ __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const
             na = nc;
             nb = force_at(frc, rc.ebase, step + 1u, 0u, 1u);
             nc = force_at(frc, rc.ebase, step + 1u, 1u, 0u);
+        }
+        if constexpr (HTRAJ == 3) {   // checkpoint: state and compensation before the step
+            if (out && act && step % (unsigned)a.traj_every == 0u) {
+                R* ck = a.traj + (long long)(step / (unsigned)a.traj_every) * 2 * N * B;
+                sl.store_vec(Q, ck, B, b);
+                sl.store_vec(Cm, ck + (long long)N * B, B, b);
+            }
         }
         if constexpr (HTRAJ == 2)
             ws_step<R, KAHAN, adj_slot_vecs<R>()>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act,
@@ -1184,6 +1210,7 @@ __device__ __forceinline__ void ws_fwd(SL& sl, const FwdArgs<R>& a, R* sm, int b
     sl.load_vec(Q, a.state, B, b);
 #pragma unroll
     for (int i = 0; i < SL::MM; ++i) { Cm[i] = R(0); Mx[i] = R(0); }
+    if (KAHAN && a.comp) sl.load_vec(Cm, a.comp, B, b);   // restart from a checkpoint
     R sq = R(0), sqc = R(0);
     RunCtx rc;
     rc.ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
@@ -1350,7 +1377,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     for (int k = khi; k >= klo; --k) {
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
-        const int slot0 = a.stored ? 0 : start;   // buf slot of step t: t - slot0
+        const int slot0 = a.stored ? a.slot_base : start;   // buf slot of step t: t - slot0
         if (!a.stored) {
             const R* ck = a.ckpt + (long long)k * 2 * N * B;
             sl.load_vec(Q, ck, B, b);
@@ -1366,7 +1393,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                                       a.buf + (long long)(t - start) * SV * N * B, (long long)N * B, B, b, valid);
             }
         } else {
-            sl.load_vec(Q, a.buf + (long long)end * SV * N * B, B, b);
+            sl.load_vec(Q, a.buf + (long long)(end - slot0) * SV * N * B, B, b);
         }
 #pragma unroll
         for (int i = 0; i < MM; ++i) QN[i] = Q[i];
@@ -1391,8 +1418,8 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
         R fc = force_at(a.frc, ebase, (unsigned)(end - 1), 1u, 0u);
         for (int t = end - 1; t >= start; --t) {
             V QC, Y2, Y3, Y4, QB, KB, YB;
-            if (a.stored && t >= kPrefetchSteps) {
-                const R* pf = a.buf + (long long)(t - kPrefetchSteps) * SV * N * B;
+            if (a.stored && t - kPrefetchSteps >= slot0) {
+                const R* pf = a.buf + (long long)(t - kPrefetchSteps - slot0) * SV * N * B;
 #pragma unroll
                 for (int j = 0; j < SV; ++j) sl.prefetch_vec(pf + (long long)j * N * B, B, b);
             }

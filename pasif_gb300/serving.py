@@ -186,7 +186,7 @@ def adjoint_bytes(pattern: Pattern, n_sys: int, nsteps: int, table: int, precisi
     else:
         c = max(1, math.ceil(math.sqrt(max(nsteps, 1))))
         nck = max(1, -(-nsteps // c))
-        traj = 2 * n * nck + sv * c * n
+        traj = 2 * n * nck + (sv * c + 1) * n + n   # checkpoints, a chunk's slots, the replay state
     per_sys = rs * (P + 3 * n + traj + 16 * n + 2) + 8 * (P + n)
     return int(n_sys * per_sys + rs * table + 4 * n_sys)
 

@@ -161,3 +161,34 @@ def test_adjoint_storage_limit_validated(gpu):
         b.adjoint_storage(-1)
     assert e.value.code == N.ERR_INVALID
     b.adjoint_storage(0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
+@pytest.mark.parametrize("seed,W,N", [(0, 2, 97), (1, 0, 144), (2, 4, 230)])
+def test_adjoint_replayed_matches(gpu, prec, seed, W, N):
+    """Checkpointed adjoint replayed by the forward kernel (checkpoint pass,
+    then per chunk its slots from the checkpoint with the Kahan compensation):
+    FP64 equals the oracle bit for bit; both precisions equal the stored
+    trajectory's gradients.  Signals shorter than the run, horizons not a
+    multiple of the chunk."""
+    rng = np.random.default_rng(320 + seed)
+    pat, v = cases.random_system(rng)
+    B = 70
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    x = cases.signals(rng, 2, 60)
+    exc = rng.integers(0, 2, B)
+    gf = rng.normal(size=(B, pat.n))
+    gs = rng.normal(size=B)
+    im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
+    out = []
+    for storage in (0, 1 << 30):
+        b = Batch(Plan(pat, prec), vals, x0, exc)
+        b.adjoint_storage(storage)
+        out.append(b.adjoint(Signals(x, W, im, prec), 0.03, N, g_final=gf, g_sq=gs, sq_comp=(0,), sq_start=N // 3))
+        assert b.kernel_info()["adjoint"] == "specialised"
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    if prec == "fp64":
+        odv, odx = O.batch_adjoint(pat, vals, x0, exc, x, 0.03, N, W, im, gf, gs, (0,), N // 3)
+        np.testing.assert_array_equal(out[0][0], odv)
+        np.testing.assert_array_equal(out[0][1], odx)

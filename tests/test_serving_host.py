@@ -203,7 +203,8 @@ def test_adjoint_bytes_stored_or_checkpointed():
     ck = S.adjoint_bytes(PAT, B, N, 10, "fp32_kahan")
     full = B * (N + 1) * n * 4
     st = S.adjoint_bytes(PAT, B, N, 10, "fp32_kahan", storage=full)
-    assert st - ck == full - B * 4 * (2 * n * 32 + 32 * n)   # ceil(sqrt(1000)) = 32 steps per chunk, 32 chunks
+    # ceil(sqrt(1000)) = 32 steps per chunk, 32 chunks: checkpoints, 33 chunk slots, the replay state
+    assert st - ck == full - B * 4 * (2 * n * 32 + 33 * n + n)
     assert S.adjoint_bytes(PAT, B, N, 10, "fp32_kahan", storage=full - 1) == ck
     full64 = B * (4 * N + 1) * n * 8
     assert S.adjoint_bytes(PAT, B, N, 10, "fp64", storage=full64) > S.adjoint_bytes(PAT, B, N, 10, "fp64")

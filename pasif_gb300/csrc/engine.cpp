@@ -514,8 +514,13 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     JitKernel fk, ckk;
     std::string ferr;
     const bool stored = jit && adj_stores(B, nsteps) && fwd_kernel(sig, 0ull, 0ull, 2, &fk, &ferr);
-    const bool replayed = !stored && jit && nsteps > 0 && fwd_kernel(sig, 0ull, 0ull, 2, &fk, &ferr) &&
-                          fwd_kernel(sig, 0ull, 0ull, 3, &ckk, &ferr);
+    // replay only grids of 32 blocks or more: a small grid runs as one launch
+    // (each of its many short replay launches would wait again for SMs that
+    // other streams' work holds: 1-DOF adjoints in the served mix took 14 s
+    // instead of 1.3 s)
+    const long long adj_blocks = jit ? (B + jk.per_block - 1) / jk.per_block : 0;
+    const bool replayed = !stored && jit && nsteps > 0 && adj_blocks >= 32 &&
+                          fwd_kernel(sig, 0ull, 0ull, 2, &fk, &ferr) && fwd_kernel(sig, 0ull, 0ull, 3, &ckk, &ferr);
     const size_t vec = Bn * (size_t)n * rs;
     if (stored) {
         PK_CUDA(buf.ensure((slot_vecs() * (size_t)nsteps + 1) * vec), "cudaMalloc");
@@ -590,10 +595,11 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
             for (int k = nck - 1; k >= 0; --k) {
                 const int t0 = k * C, t1 = std::min(nsteps, t0 + C);
                 const char* ck = static_cast<const char*>(ckpt.p) + (size_t)k * 2 * n * Bn * rsz;
-                cudaError_t le = cudaMemcpyAsync(adj_state.p, ck, vec, cudaMemcpyDeviceToDevice, st);
-                if (le != cudaSuccess) return le;
-                le = launch_fwd_jit(fk, sig, h, t0, t1 - t0, Reducers(), 0ull, 0ull, 1, t1 - t0, adj_state.p, buf.p,
-                                    st, ck + (size_t)n * Bn * rsz);
+                // the forward runs on the checkpoint's state in place (no copy: with many
+                // adjoints in flight, a copy per chunk queued behind the others' copies);
+                // chunk k's checkpoint is not read again
+                cudaError_t le = launch_fwd_jit(fk, sig, h, t0, t1 - t0, Reducers(), 0ull, 0ull, 1, t1 - t0,
+                                                const_cast<char*>(ck), buf.p, st, ck + (size_t)n * Bn * rsz);
                 if (le != cudaSuccess) return le;
                 a.phase = 2;
                 a.k_hi = a.k_lo = k;

@@ -143,21 +143,19 @@ bool to_cubin(const std::string& src, std::vector<char>* cubin, std::string* log
     return true;
 }
 
-bool compile(const std::string& src, const char* name, cudaKernel_t* fn, std::string* err) {
+bool compile(const std::string& src, const char* name, cudaKernel_t* fn, cudaLibrary_t* lib, std::string* err) {
     std::vector<char> cubin;
     if (!to_cubin(src, &cubin, nullptr, err)) return false;
-    cudaLibrary_t lib;
-    cudaError_t ce = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    cudaError_t ce = cudaLibraryLoadData(lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (ce != cudaSuccess) {
         *err = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(ce);
         return false;
     }
-    ce = cudaLibraryGetKernel(fn, lib, name);
+    ce = cudaLibraryGetKernel(fn, *lib, name);
     if (ce != cudaSuccess) {
         *err = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(ce);
         return false;
     }
-    cache().libs.push_back(lib);
     return true;
 }
 
@@ -727,13 +725,19 @@ void emit_vjp(std::ostringstream& o, const Pattern& pat, const Emitter& em) {
     o << "  }\n";
 }
 
+// The cache lock is not held while NVRTC compiles (up to a second for a large
+// pattern): the host threads of a server keep launching cached kernels while
+// another thread compiles a new one.  Two threads compiling the same source
+// both load it; the first to finish is the one kept.
 bool get_cached(const std::string& src, const char* name, int block, JitKernel* out, std::string* err) {
     Cache& c = cache();
-    std::lock_guard<std::mutex> lk(c.mu);
-    auto it = c.fwd.find(src);
-    if (it != c.fwd.end()) {
-        *out = it->second;
-        return true;
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        auto it = c.fwd.find(src);
+        if (it != c.fwd.end()) {
+            *out = it->second;
+            return true;
+        }
     }
     JitKernel k;
     k.block = block;
@@ -742,7 +746,8 @@ bool get_cached(const std::string& src, const char* name, int block, JitKernel* 
         ws_launch(src, &k.block, &k.smem);
         k.per_block = 32;
     }
-    if (!compile(src, name, &k.fn, err)) return false;
+    cudaLibrary_t lib;
+    if (!compile(src, name, &k.fn, &lib, err)) return false;
     if (k.smem > 48 * 1024) {
         cudaError_t ce = cudaFuncSetAttribute((const void*)k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem);
         if (ce != cudaSuccess) {
@@ -754,6 +759,13 @@ bool get_cached(const std::string& src, const char* name, int block, JitKernel* 
     if (cudaFuncGetAttributes(&attr, (const void*)k.fn) == cudaSuccess) {
         k.regs = attr.numRegs;
         k.local_bytes = (int)attr.localSizeBytes;
+    }
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.libs.push_back(lib);   // loaded for the life of the process
+    auto it = c.fwd.find(src);
+    if (it != c.fwd.end()) {   // another thread finished the same compile first
+        *out = it->second;
+        return true;
     }
     c.fwd[src] = k;
     *out = k;

@@ -288,6 +288,12 @@ class Server:
                         self._worker_objs[(k, i)] = self._adjoint_objects(spec, rq, None)
                     sig, b = self._worker_objs[(k, 0)]   # compile the adjoint kernel
                     b.adjoint(sig, spec.h, rq.nsteps, g_sq=np.ones(1), sq_comp=spec.positions, sq_start=0)
+                    # and the forward kernels that replay the checkpoints of large requests
+                    m = min(int(self.reserve[0]), 4096)
+                    b.adjoint_storage(0)
+                    b.set(np.zeros((m, P)), np.zeros((m, n)), np.zeros(m, np.int32))
+                    b.adjoint(sig, spec.h, 8, g_sq=np.ones(m), sq_comp=spec.positions, sq_start=0)
+                    b.adjoint_storage(self.adjoint_storage)
                 else:
                     self._adjoint_runner(spec, rq, None)
 

@@ -170,10 +170,11 @@ def test_adjoint_replayed_matches(gpu, prec, seed, W, N):
     then per chunk its slots from the checkpoint with the Kahan compensation):
     FP64 equals the oracle bit for bit; both precisions equal the stored
     trajectory's gradients.  Signals shorter than the run, horizons not a
-    multiple of the chunk."""
+    multiple of the chunk.  4200 systems: 32 blocks or more in either layout
+    (smaller grids run the checkpoints inside the adjoint kernel)."""
     rng = np.random.default_rng(320 + seed)
     pat, v = cases.random_system(rng)
-    B = 70
+    B = 4200
     vals, x0 = cases.random_batch(rng, pat, v, B)
     x = cases.signals(rng, 2, 60)
     exc = rng.integers(0, 2, B)

@@ -163,18 +163,18 @@ def test_adjoint_storage_limit_validated(gpu):
     b.adjoint_storage(0)
 
 
+@pytest.mark.parametrize("B", [70, 4200])
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
 @pytest.mark.parametrize("seed,W,N", [(0, 2, 97), (1, 0, 144), (2, 4, 230)])
-def test_adjoint_replayed_matches(gpu, prec, seed, W, N):
+def test_adjoint_replayed_matches(gpu, prec, seed, W, N, B):
     """Checkpointed adjoint replayed by the forward kernel (checkpoint pass,
     then per chunk its slots from the checkpoint with the Kahan compensation):
     FP64 equals the oracle bit for bit; both precisions equal the stored
     trajectory's gradients.  Signals shorter than the run, horizons not a
-    multiple of the chunk.  4200 systems: 32 blocks or more in either layout
-    (smaller grids run the checkpoints inside the adjoint kernel)."""
+    multiple of the chunk.  4200 systems: 32 blocks or more in either layout;
+    70 systems: a small grid, whose checkpoints run inside the adjoint kernel."""
     rng = np.random.default_rng(320 + seed)
     pat, v = cases.random_system(rng)
-    B = 4200
     vals, x0 = cases.random_batch(rng, pat, v, B)
     x = cases.signals(rng, 2, 60)
     exc = rng.integers(0, 2, B)

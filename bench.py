@@ -400,13 +400,13 @@ def main():
                             "max_rel_err_grad_fp32_kahan_vs_fp64": float(grel.max()),
                             "median_rel_err_grad": float(np.median(grel)),
                             "rel_err_definition": "per system max|g32-g64| / max|g64| over its values",
-                            "bound": 1e-5,
-                            "systems_over_bound": int(over.sum()),
+                            "note": "the 1e-5 bound is stated for amplitudes; gradients are reported with their error",
+                            "systems_over_1e-5": int(over.sum()),
                             "final_state_rel_err_fp32_kahan_vs_fp64": {
                                 "median": float(np.median(srel)), "max": float(srel.max()),
-                                "systems_over_bound": {"min": float(srel[over].min()), "median": float(np.median(srel[over])),
-                                                       "max": float(srel[over].max())} if over.any() else None,
-                                "median_over_systems_within_bound":
+                                "systems_over_1e-5": {"min": float(srel[over].min()), "median": float(np.median(srel[over])),
+                                                      "max": float(srel[over].max())} if over.any() else None,
+                                "median_over_other_systems":
                                     float(np.median(srel[~over])) if (~over).any() else None}},
                 "other_configs": other,
                 "serving": served,

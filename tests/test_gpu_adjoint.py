@@ -193,3 +193,28 @@ def test_adjoint_replayed_matches(gpu, prec, seed, W, N, B):
         odv, odx = O.batch_adjoint(pat, vals, x0, exc, x, 0.03, N, W, im, gf, gs, (0,), N // 3)
         np.testing.assert_array_equal(out[0][0], odv)
         np.testing.assert_array_equal(out[0][1], odx)
+
+
+@pytest.mark.parametrize("storage", [0, 1 << 30])
+@pytest.mark.parametrize("N,B", [(0, 5), (1, 5), (2, 1), (3, 33)])
+def test_adjoint_short_horizons(gpu, N, B, storage):
+    """Edge horizons: no step (d x0 = g_final, no value gradient), one step,
+    a single system; FP64 equals the oracle bit for bit in every trajectory
+    mode."""
+    rng = np.random.default_rng(340 + N)
+    pat, v = cases.random_system(rng, n=3)
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    x = cases.signals(rng, 2, 20)
+    exc = rng.integers(0, 2, B)
+    gf = rng.normal(size=(B, pat.n))
+    gs = rng.normal(size=B)
+    im = [[0, .5], [1, .5]]
+    b = Batch(Plan(pat, "fp64"), vals, x0, exc)
+    b.adjoint_storage(storage)
+    dv, dx = b.adjoint(Signals(x, 2, im, "fp64"), 0.03, N, g_final=gf, g_sq=gs, sq_comp=(0,), sq_start=0)
+    odv, odx = O.batch_adjoint(pat, vals, x0, exc, x, 0.03, N, 2, im, gf, gs, (0,), 0)
+    np.testing.assert_array_equal(dv, odv)
+    np.testing.assert_array_equal(dx, odx)
+    if N == 0:
+        np.testing.assert_array_equal(dx, gf)
+        assert not dv.any()

@@ -40,7 +40,7 @@ UNIT = "system-steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--systems", type=int, default=16384)
@@ -115,13 +115,17 @@ def run_reference(args):
 
 
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+    """nvidia-smi sampling every 50 ms, started before the timed region (the
+    first query takes a while to come up); `region(t0, t1)` keeps the samples
+    stamped inside a wall-clock window (plus the first one after it)."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.window = None
         self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{index}.csv")
 
     def __enter__(self):
@@ -129,11 +133,16 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
+            time.sleep(0.5)   # nvidia-smi's first query takes a while to come up
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
+
+    def region(self, t0, t1):
+        """Wall-clock window (datetime.now() values) of the timed region."""
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -147,22 +156,26 @@ class ClockSampler:
     def summary(self):
         if self.proc is None or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        from datetime import datetime
+        rows = []
         for line in open(self.path):
             p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
+            if len(p) < 10:
                 continue
             try:
-                sm.append(float(p[1]))
-                smax = float(p[2])
+                rows.append((datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f"), float(p[2]), float(p[3]), p[6:10]))
             except ValueError:
                 continue
-            for name, val in zip(names, p[5:9]):
-                if val.lower() == "active":
-                    reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        if self.window is not None:
+            t0, t1 = self.window
+            inside = [r for r in rows if t0 <= r[0] <= t1]
+            after = [r for r in rows if r[0] > t1][:1]   # covers the region's last interval
+            rows = inside + after
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = {name for r in rows for name, val in zip(names, r[3]) if val.lower() == "active"}
+        sm = [r[1] for r in rows]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": rows[-1][2] if rows else None,
+                "reasons": sorted(reasons), "samples": len(sm), "interval_ms": 50}
 
 
 def main():
@@ -195,20 +208,21 @@ def main():
     def solve():
         batch.forward(sig, w.h, w.nsteps, stream=stream)
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            solve()
-    torch.cuda.synchronize()
-    info = batch.kernel_info()
-
     def barrier():
         if dist is not None:
             dist.barrier()
 
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
+    from datetime import datetime
+    with ClockSampler(local) as clk:   # sampling from before the warm-up solves
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                solve()
+        torch.cuda.synchronize()
+        info = batch.kernel_info()
         barrier()
         torch.cuda.synchronize()
+        d_start = datetime.now()
         t_wall = time.perf_counter()
         with torch.cuda.stream(stream):
             for e0, e1 in evs:
@@ -218,6 +232,7 @@ def main():
                 e1.record(stream)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
+        clk.region(d_start, datetime.now())
         barrier()
     from pasif_gb300.replicas import job_rate, max_over_ranks
     kernel_s = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in evs) * 1e-3, dist, "cuda")

@@ -121,9 +121,12 @@ bool to_cubin(const std::string& src, std::vector<char>* cubin, std::string* log
         *err = "nvrtcCreateProgram failed";
         return false;
     }
-    const char* opts[] = {"-arch=sm_103a", "-std=c++17", "--fmad=false", "-lineinfo", "-DNDEBUG",
-                          "--ptxas-options=-v"};
-    nvrtcResult rc = nvrtcCompileProgram(prog, log ? 6 : 5, opts);
+    std::vector<const char*> opts = {"-arch=sm_103a", "-std=c++17", "--fmad=false", "-lineinfo", "-DNDEBUG"};
+    // tuning override: one extra compiler option (e.g. a ptxas option)
+    const char* extra = std::getenv("PASIF_NVRTC_OPT");
+    if (extra && *extra) opts.push_back(extra);
+    if (log) opts.push_back("--ptxas-options=-v");
+    nvrtcResult rc = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
     size_t ls = 0;
     nvrtcGetProgramLogSize(prog, &ls);
     std::string text(ls, '\0');

@@ -904,11 +904,14 @@ int ws_split(int n, bool f32, bool force, bool adjoint) {
     // components per warp): each SM sub-partition then runs one slice's code.
     // Measured on GB300 (forward, FP32-Kahan): 128-state chain 4 warps 1.86e9
     // system-steps/s vs 8 warps 1.5e9, 16 warps 0.84e9; 64-state banded 1.68e9
-    // vs 1.30e9.  The adjoint holds about twice the vectors: 8 FP32 / 6 FP64
-    // components per warp, at least 4 and (FP32) at most 8 warps (gradient rates:
-    // 16-state chain 4 warps 1.32e9 vs 2 warps 1.01e9; 128-state chain 8 warps
-    // 1.35e8 vs 16 warps 0.98e8).
-    const int cpw = force ? 2 : adjoint ? (f32 ? 8 : 6) : (f32 ? 32 : 16);   // components per warp
+    // vs 1.30e9.  The adjoint holds about twice the vectors: 11 FP32 / 6 FP64
+    // components per warp, at least 4 and (FP32) at most 8 warps.  Gradient
+    // rates: 16-state chain 4 warps 1.32e9 vs 2 warps 1.01e9; 128-state chain 8
+    // warps 1.35e8 vs 16 warps 0.98e8.  FP32 adjoint of 4096 systems (M adjoint
+    // system-steps/s): 64-state banded 6 warps 208, 8 warps 176, 12 warps 119;
+    // 32-state chain 4 warps 770, 6 warps 740; 128-state chain 8 warps 134, 12
+    // warps 89.  (512 systems, 16 blocks, prefer more warps by 5-10 %.)
+    const int cpw = force ? 2 : adjoint ? (f32 ? 11 : 6) : (f32 ? 32 : 16);   // components per warp
     int L = std::max(4, (n + cpw - 1) / cpw);
     if (adjoint && f32 && !force) L = std::min(L, 8);
     if (const char* e = std::getenv("PASIF_WS_SLICES")) L = std::atoi(e);   // tuning override

@@ -88,7 +88,8 @@ def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N,
     mask = sum(1 << c for c in sq)
     src = Plan(pat, prec, slicing=slicing).jit_report_adjoint(vals, sq_mask=mask)
     src = src.split("// ---- source ----\n", 1)[1]
-    assert ("warp-sliced" in src) == bool(slicing)
+    if slicing is not None:
+        assert ("warp-sliced" in src) == bool(slicing)
     exe, env = build_emulator(d, src, "EMU_ADJ")
     if split:
         env["EMU_ADJ_SPLIT"] = str(split)
@@ -273,6 +274,28 @@ def test_generated_warp_sliced_banded32(tmp_path, prec):
     ref, _, _ = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
                                 prec)
     np.testing.assert_array_equal(got, ref)
+
+
+
+def test_generated_adjoint_banded32_default_slices(tmp_path):
+    """64-state banded system, FP32-Kahan: the default warp-sliced adjoint
+    (6 warps of 10-11 components) gives the bits of a 16-warp split."""
+    w = synth.banded32(n_sys=5, nsteps=30, sig_len=64)
+    rng = np.random.default_rng(31)
+    gf = rng.normal(size=(w.n_sys, w.pattern.n))
+    gs = rng.normal(size=w.n_sys)
+    sq, N = (0, 5), 30
+    rep = Plan(w.pattern, "fp32_kahan").jit_report_adjoint(w.values, sq_mask=(1 << 0) | (1 << 5))
+    assert "slices=6 " in rep.split("// ---- source ----\n", 1)[1].splitlines()[0]
+    out = []
+    for slicing in (None, True):
+        d = os.path.join(str(tmp_path), str(slicing))
+        os.makedirs(d)
+        out.append(run_emulated_adjoint(d, w.pattern, "fp32_kahan", slicing, w.values, w.x0, w.exc_index, w.signals,
+                                        np.asarray(w.im), gf, gs, N, sq, N // 3, h=w.h))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert np.abs(out[0][0]).max() > 0
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])

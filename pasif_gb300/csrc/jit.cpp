@@ -157,6 +157,7 @@ bool compile(const std::string& src, const char* name, cudaKernel_t* fn, cudaLib
     ce = cudaLibraryGetKernel(fn, *lib, name);
     if (ce != cudaSuccess) {
         *err = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(ce);
+        cudaLibraryUnload(*lib);
         return false;
     }
     return true;
@@ -755,6 +756,7 @@ bool get_cached(const std::string& src, const char* name, int block, JitKernel* 
         cudaError_t ce = cudaFuncSetAttribute((const void*)k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem);
         if (ce != cudaSuccess) {
             *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ce);
+            cudaLibraryUnload(lib);
             return false;
         }
     }
@@ -764,12 +766,13 @@ bool get_cached(const std::string& src, const char* name, int block, JitKernel* 
         k.local_bytes = (int)attr.localSizeBytes;
     }
     std::lock_guard<std::mutex> lk(c.mu);
-    c.libs.push_back(lib);   // loaded for the life of the process
     auto it = c.fwd.find(src);
-    if (it != c.fwd.end()) {   // another thread finished the same compile first
+    if (it != c.fwd.end()) {   // another thread finished the same compile first: keep its kernel
+        cudaLibraryUnload(lib);
         *out = it->second;
         return true;
     }
+    c.libs.push_back(lib);   // loaded for the life of the process
     c.fwd[src] = k;
     *out = k;
     return true;

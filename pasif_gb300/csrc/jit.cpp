@@ -766,13 +766,15 @@ bool get_cached(const std::string& src, const char* name, int block, JitKernel* 
         k.local_bytes = (int)attr.localSizeBytes;
     }
     std::lock_guard<std::mutex> lk(c.mu);
+    // loaded for the life of the process, the copy of a compile that another
+    // thread finished first too (unloading a module may wait for the device,
+    // which would stall the other threads' streams)
+    c.libs.push_back(lib);
     auto it = c.fwd.find(src);
-    if (it != c.fwd.end()) {   // another thread finished the same compile first: keep its kernel
-        cudaLibraryUnload(lib);
+    if (it != c.fwd.end()) {
         *out = it->second;
         return true;
     }
-    c.libs.push_back(lib);   // loaded for the life of the process
     c.fwd[src] = k;
     *out = k;
     return true;

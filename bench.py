@@ -163,10 +163,14 @@ class ClockSampler:
             if len(p) < 10:
                 continue
             try:
-                rows.append((datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f"), float(p[2]), float(p[3]), p[6:10]))
+                stamp = datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                stamp = None   # unexpected timestamp format: the sample is kept unfiltered
+            try:
+                rows.append((stamp, float(p[2]), float(p[3]), p[6:10]))
             except ValueError:
                 continue
-        if self.window is not None:
+        if self.window is not None and all(r[0] is not None for r in rows):
             t0, t1 = self.window
             inside = [r for r in rows if t0 <= r[0] <= t1]
             after = [r for r in rows if r[0] > t1][:1]   # covers the region's last interval

@@ -56,3 +56,14 @@ def test_clock_summary_without_nvidia_smi(tmp_path):
     c.path = str(tmp_path / "missing.csv")
     s = c.summary()
     assert s["sm_mhz"] is None and s["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_clock_summary_unparsed_timestamps_keep_every_sample(tmp_path):
+    path = tmp_path / "c.csv"
+    path.write_text("Fri Dec 4 06:22:03 2026, 0, 2070, 2070, 900.0, 0x0, Not Active, Not Active, Not Active, "
+                    "Not Active\n" * 3)
+    c = _sampler(path)
+    t0 = datetime.datetime(2026, 1, 2)
+    c.region(t0, t0 + datetime.timedelta(seconds=1))
+    s = c.summary()
+    assert s["samples"] == 3 and s["sm_mhz"] == 2070.0

@@ -384,19 +384,29 @@ class Server:
                     if self._stop:
                         return
                     pending = list(q)
-                admitted = 0
+                consumed, refused = 0, []
                 for req, res in pending:      # first come, first served; stop at the first that does not fit
-                    rid = pool.admit(req.values, req.x0, req.exc_index, req.signals, req.nsteps, req.max_start,
-                                     req.sq_start)
+                    try:
+                        rid = pool.admit(req.values, req.x0, req.exc_index, req.signals, req.nsteps,
+                                         req.max_start, req.sq_start)
+                    except N.PasifError as e:   # this request is invalid; the pool goes on
+                        refused.append((res, f"forward refused: {e}"))
+                        consumed += 1
+                        continue
                     if rid is None:
+                        if not running and consumed == 0:   # does not fit an idle pool: never will
+                            refused.append((res, "request does not fit an idle serving pool"))
+                            consumed += 1
                         break
                     res.t_admit = self.now()
                     running[rid] = (req, res)
-                    admitted += 1
-                if admitted:
+                    consumed += 1
+                if consumed:
                     with self._cv:
-                        for _ in range(admitted):
+                        for _ in range(consumed):
                             q.popleft()
+                for res, err in refused:
+                    self._finish(res, error=err)
                 if not running:
                     continue
                 pool.launch()

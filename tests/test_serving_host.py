@@ -8,6 +8,7 @@ import time
 import numpy as np
 import pytest
 
+from pasif_gb300 import _native as N
 from pasif_gb300 import serving as S
 from pasif_gb300.system import Pattern
 
@@ -25,6 +26,8 @@ class FakePool:
 
     def admit(self, values, x0, exc_index, signals, nsteps, max_start=0, sq_start=0):
         m, t = len(values), np.asarray(signals).size
+        if nsteps < 0:   # as pasif_pool_admit: invalid input is an error, not a wait
+            raise N.PasifError(N.ERR_INVALID, "negative step count")
         if m > self.free or t > self.arena - self.used_arena:
             return None
         rid, self.next = self.next, self.next + 1
@@ -92,6 +95,22 @@ def test_arena_limits_admission():
     assert res[9].error is not None
     assert all(res[i].error is None for i in range(4))
 
+
+
+def test_invalid_forward_request_fails_alone():
+    """A request the pool rejects as invalid gets an error result; the
+    class's pool goes on serving the others."""
+    srv, log = make_server()
+    srv.start()
+    srv.submit(req(0, "forward", 2))
+    srv.submit(req(1, "forward", 2, nsteps=-5))
+    srv.submit(req(2, "forward", 3))
+    assert srv.wait(10.0)
+    srv.stop()
+    res = srv.results()
+    assert res[1].error and "forward refused" in res[1].error
+    assert res[0].error is None and res[2].error is None
+    np.testing.assert_array_equal(res[2].state, np.full((3, 2), 4.0))
 
 def test_adjoint_budget():
     lock, state = threading.Lock(), {"now": 0, "peak": 0}

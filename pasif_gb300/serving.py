@@ -323,13 +323,14 @@ class Server:
         return self.clock() - self.t0
 
     def submit(self, req: Request) -> None:
-        res = Result(req.rid, req.kind, self.now())
+        n_sys = req.n_sys   # a malformed request raises here, before it is registered
         table = int(np.asarray(req.signals).size)
+        res = Result(req.rid, req.kind, self.now())
         with self._cv:
             self._results[req.rid] = res
             self._outstanding += 1
         if req.kind == "forward":
-            if req.n_sys > self.capacity or table > self.arena_samples:
+            if n_sys > self.capacity or table > self.arena_samples:
                 return self._finish(res, error="request larger than a serving pool (slots or signal arena)")
             self._pool(req.cls)
             with self._cv:
@@ -337,7 +338,7 @@ class Server:
                 self._cv.notify_all()
         elif req.kind == "adjoint":
             spec = self.specs[req.cls]
-            need = adjoint_bytes(spec.pattern, req.n_sys, req.nsteps, table, self.precision, self.adjoint_storage)
+            need = adjoint_bytes(spec.pattern, n_sys, req.nsteps, table, self.precision, self.adjoint_storage)
             if need > self.adjoint_budget:
                 return self._finish(res, error=f"adjoint needs {need} bytes, budget {self.adjoint_budget}")
             with self._cv:
@@ -389,7 +390,7 @@ class Server:
                     try:
                         rid = pool.admit(req.values, req.x0, req.exc_index, req.signals, req.nsteps,
                                          req.max_start, req.sq_start)
-                    except N.PasifError as e:   # this request is invalid; the pool goes on
+                    except (N.PasifError, ValueError, TypeError) as e:   # invalid request; the pool goes on
                         refused.append((res, f"forward refused: {e}"))
                         consumed += 1
                         continue
@@ -440,7 +441,7 @@ class Server:
                 err = None
                 try:
                     res.d_values, res.d_x0 = self._adjoint_runner(self.specs[req.cls], req, stream)
-                except N.PasifError as e:      # this request failed; the worker goes on
+                except (N.PasifError, ValueError, TypeError) as e:   # this request failed; the worker goes on
                     err = f"adjoint failed: {e}"
                 finally:
                     with self._cv:

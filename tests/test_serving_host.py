@@ -28,6 +28,7 @@ class FakePool:
         m, t = len(values), np.asarray(signals).size
         if nsteps < 0:   # as pasif_pool_admit: invalid input is an error, not a wait
             raise N.PasifError(N.ERR_INVALID, "negative step count")
+        np.asarray(x0, dtype=float).reshape(m, 2)   # as Pool.admit's shape checks
         if m > self.free or t > self.arena - self.used_arena:
             return None
         rid, self.next = self.next, self.next + 1
@@ -105,10 +106,17 @@ def test_invalid_forward_request_fails_alone():
     srv.submit(req(0, "forward", 2))
     srv.submit(req(1, "forward", 2, nsteps=-5))
     srv.submit(req(2, "forward", 3))
+    bad = req(3, "forward", 2)
+    bad.x0 = np.zeros((3, 2))   # three initial states for two systems
+    srv.submit(bad)
+    with pytest.raises(AttributeError):   # not a request at all: raised to the caller, not registered
+        srv.submit(S.Request(4, "forward", "a", "not an array", None, None, np.zeros((1, 4)), 10))
     assert srv.wait(10.0)
     srv.stop()
     res = srv.results()
     assert res[1].error and "forward refused" in res[1].error
+    assert res[3].error and "forward refused" in res[3].error
+    assert 4 not in res
     assert res[0].error is None and res[2].error is None
     np.testing.assert_array_equal(res[2].state, np.full((3, 2), 4.0))
 

@@ -237,17 +237,6 @@ int Pool::admit(int n_sys, const double* values, const double* x0, const int* ex
         if (exc_index[i] < 0 || exc_index[i] >= n_exc) { *err = "excitation index out of range"; return 1; }
     const long long table = (long long)n_exc * len;
     if (n_sys > C_ || table > S_) { *err = "request larger than the pool (slots or signal arena)"; return 1; }
-    if ((int)free_.size() < n_sys) { *err = "pool full"; return 5; }
-    const long long off = arena_alloc(table);
-    if (off < 0) { *err = "signal arena full"; return 5; }
-    PoolRequest r;
-    r.n_sys = n_sys;
-    r.arena_off = off;
-    r.arena_len = table;
-    for (int i = 0; i < n_sys; ++i) {
-        r.slots.push_back(free_.back());
-        free_.pop_back();
-    }
     const bool f32 = plan_->precision != kFP64;
     // staging: values, x0, zeros, signals (double) | slots, step, remain, mstart, sstart (int) | ebase, lim (i64) | len (u32)
     auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
@@ -259,51 +248,80 @@ int Pool::admit(int n_sys, const double* values, const double* x0, const int* ex
     const size_t o_ms = al(o_rem + sizeof(int) * n_sys), o_ss = al(o_ms + sizeof(int) * n_sys);
     const size_t o_eb = al(o_ss + sizeof(int) * n_sys), o_lim = al(o_eb + sizeof(long long) * n_sys);
     const size_t o_len = al(o_lim + sizeof(long long) * n_sys), total = al(o_len + sizeof(unsigned) * n_sys);
-    std::vector<unsigned char> host(total, 0);
-    std::memcpy(&host[o_vals], values, sizeof(double) * (size_t)n_sys * P);
-    std::memcpy(&host[o_x0], x0, sizeof(double) * (size_t)n_sys * n);
-    std::memcpy(&host[o_sig], signals, sizeof(double) * (size_t)table);
+    PL_CUDA(scratch_.ensure(total), "cudaMalloc");   // before any slot or arena space is taken
+    if ((int)free_.size() < n_sys) { *err = "pool full"; return 5; }
+    const long long off = arena_alloc(table);
+    if (off < 0) { *err = "signal arena full"; return 5; }
+    PoolRequest r;
+    r.n_sys = n_sys;
+    r.arena_off = off;
+    r.arena_len = table;
     for (int i = 0; i < n_sys; ++i) {
-        reinterpret_cast<int*>(&host[o_slots])[i] = r.slots[i];
-        reinterpret_cast<unsigned*>(&host[o_step])[i] = 0u;
-        reinterpret_cast<int*>(&host[o_rem])[i] = nsteps;
-        reinterpret_cast<int*>(&host[o_ms])[i] = max_start;
-        reinterpret_cast<int*>(&host[o_ss])[i] = sq_start;
-        reinterpret_cast<long long*>(&host[o_eb])[i] = off + (long long)exc_index[i] * len;
-        reinterpret_cast<long long*>(&host[o_lim])[i] = off + table;
-        reinterpret_cast<unsigned*>(&host[o_len])[i] = (unsigned)len;
+        r.slots.push_back(free_.back());
+        free_.pop_back();
     }
-    PL_CUDA(scratch_.ensure(total), "cudaMalloc");
-    unsigned char* d = scratch_.as<unsigned char>();
-    PL_CUDA(cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, st_), "cudaMemcpyAsync");
-    const int* dslots = reinterpret_cast<const int*>(d + o_slots);
-    const double* dz = reinterpret_cast<const double*>(d + o_zero);
-    const long long Cl = C_;
-    PL_CUDA(pk::launch_scatter_cols(reinterpret_cast<const double*>(d + o_vals), vals_.p, dslots, n_sys, P, Cl, f32, st_),
-            "scatter");
-    PL_CUDA(pk::launch_scatter_cols(reinterpret_cast<const double*>(d + o_x0), state_.p, dslots, n_sys, n, Cl, f32, st_),
-            "scatter");
-    PL_CUDA(pk::launch_scatter_cols(dz, comp_.p, dslots, n_sys, n, Cl, f32, st_), "scatter");
-    PL_CUDA(pk::launch_scatter_cols(dz, mx_.p, dslots, n_sys, n, Cl, f32, st_), "scatter");
-    PL_CUDA(pk::launch_scatter_cols(dz, sq_.p, dslots, n_sys, 1, Cl, f32, st_), "scatter");
-    PL_CUDA(pk::launch_scatter_cols(dz, sqc_.p, dslots, n_sys, 1, Cl, f32, st_), "scatter");
-    const size_t rs = f32 ? sizeof(float) : sizeof(double);
-    PL_CUDA(pk::launch_convert(reinterpret_cast<const double*>(d + o_sig), arena_.as<unsigned char>() + (size_t)off * rs,
-                               table, f32, st_),
-            "convert");
-    PL_CUDA(pk::launch_scatter_u32(reinterpret_cast<const unsigned*>(d + o_step), step_.as<unsigned>(), dslots, n_sys, st_),
-            "scatter");
-    PL_CUDA(pk::launch_scatter_i32(reinterpret_cast<const int*>(d + o_ms), mstart_.as<int>(), dslots, n_sys, st_), "scatter");
-    PL_CUDA(pk::launch_scatter_i32(reinterpret_cast<const int*>(d + o_ss), sstart_.as<int>(), dslots, n_sys, st_), "scatter");
-    PL_CUDA(pk::launch_scatter_i64(reinterpret_cast<const long long*>(d + o_eb), ebase_.as<long long>(), dslots, n_sys, st_),
-            "scatter");
-    PL_CUDA(pk::launch_scatter_i64(reinterpret_cast<const long long*>(d + o_lim), lim_.as<long long>(), dslots, n_sys, st_),
-            "scatter");
-    PL_CUDA(pk::launch_scatter_u32(reinterpret_cast<const unsigned*>(d + o_len), len_.as<unsigned>(), dslots, n_sys, st_),
-            "scatter");
-    // remain last: the slot becomes busy only when everything else is in place
-    PL_CUDA(pk::launch_scatter_i32(reinterpret_cast<const int*>(d + o_rem), remain_.as<int>(), dslots, n_sys, st_), "scatter");
-    PL_CUDA(cudaStreamSynchronize(st_), "cudaStreamSynchronize");   // staging reused by the next admission
+    // upload and scatter into the slots; `remain` last, so a slot becomes busy
+    // only when everything else is in place
+    auto stage = [&]() -> int {
+        std::vector<unsigned char> host(total, 0);
+        std::memcpy(&host[o_vals], values, sizeof(double) * (size_t)n_sys * P);
+        std::memcpy(&host[o_x0], x0, sizeof(double) * (size_t)n_sys * n);
+        std::memcpy(&host[o_sig], signals, sizeof(double) * (size_t)table);
+        for (int i = 0; i < n_sys; ++i) {
+            reinterpret_cast<int*>(&host[o_slots])[i] = r.slots[i];
+            reinterpret_cast<unsigned*>(&host[o_step])[i] = 0u;
+            reinterpret_cast<int*>(&host[o_rem])[i] = nsteps;
+            reinterpret_cast<int*>(&host[o_ms])[i] = max_start;
+            reinterpret_cast<int*>(&host[o_ss])[i] = sq_start;
+            reinterpret_cast<long long*>(&host[o_eb])[i] = off + (long long)exc_index[i] * len;
+            reinterpret_cast<long long*>(&host[o_lim])[i] = off + table;
+            reinterpret_cast<unsigned*>(&host[o_len])[i] = (unsigned)len;
+        }
+        unsigned char* d = scratch_.as<unsigned char>();
+        PL_CUDA(cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, st_), "cudaMemcpyAsync");
+        const int* dslots = reinterpret_cast<const int*>(d + o_slots);
+        const double* dz = reinterpret_cast<const double*>(d + o_zero);
+        const long long Cl = C_;
+        PL_CUDA(pk::launch_scatter_cols(reinterpret_cast<const double*>(d + o_vals), vals_.p, dslots, n_sys, P, Cl, f32,
+                                        st_),
+                "scatter");
+        PL_CUDA(pk::launch_scatter_cols(reinterpret_cast<const double*>(d + o_x0), state_.p, dslots, n_sys, n, Cl, f32,
+                                        st_),
+                "scatter");
+        PL_CUDA(pk::launch_scatter_cols(dz, comp_.p, dslots, n_sys, n, Cl, f32, st_), "scatter");
+        PL_CUDA(pk::launch_scatter_cols(dz, mx_.p, dslots, n_sys, n, Cl, f32, st_), "scatter");
+        PL_CUDA(pk::launch_scatter_cols(dz, sq_.p, dslots, n_sys, 1, Cl, f32, st_), "scatter");
+        PL_CUDA(pk::launch_scatter_cols(dz, sqc_.p, dslots, n_sys, 1, Cl, f32, st_), "scatter");
+        const size_t rs = f32 ? sizeof(float) : sizeof(double);
+        PL_CUDA(pk::launch_convert(reinterpret_cast<const double*>(d + o_sig),
+                                   arena_.as<unsigned char>() + (size_t)off * rs, table, f32, st_),
+                "convert");
+        PL_CUDA(pk::launch_scatter_u32(reinterpret_cast<const unsigned*>(d + o_step), step_.as<unsigned>(), dslots, n_sys,
+                                       st_),
+                "scatter");
+        PL_CUDA(pk::launch_scatter_i32(reinterpret_cast<const int*>(d + o_ms), mstart_.as<int>(), dslots, n_sys, st_),
+                "scatter");
+        PL_CUDA(pk::launch_scatter_i32(reinterpret_cast<const int*>(d + o_ss), sstart_.as<int>(), dslots, n_sys, st_),
+                "scatter");
+        PL_CUDA(pk::launch_scatter_i64(reinterpret_cast<const long long*>(d + o_eb), ebase_.as<long long>(), dslots,
+                                       n_sys, st_),
+                "scatter");
+        PL_CUDA(pk::launch_scatter_i64(reinterpret_cast<const long long*>(d + o_lim), lim_.as<long long>(), dslots,
+                                       n_sys, st_),
+                "scatter");
+        PL_CUDA(pk::launch_scatter_u32(reinterpret_cast<const unsigned*>(d + o_len), len_.as<unsigned>(), dslots, n_sys,
+                                       st_),
+                "scatter");
+        PL_CUDA(pk::launch_scatter_i32(reinterpret_cast<const int*>(d + o_rem), remain_.as<int>(), dslots, n_sys, st_),
+                "scatter");
+        PL_CUDA(cudaStreamSynchronize(st_), "cudaStreamSynchronize");   // staging reused by the next admission
+        return 0;
+    };
+    if (const int rc = stage()) {   // the slots and the arena space go back to the pool
+        for (auto it = r.slots.rbegin(); it != r.slots.rend(); ++it) free_.push_back(*it);
+        arena_free(off, table);
+        return rc;
+    }
     *req_id = next_id_++;
     reqs_[*req_id] = r;
     return 0;

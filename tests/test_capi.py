@@ -50,6 +50,15 @@ def test_invalid_pattern_is_rejected_before_cuda():
 def test_null_handles():
     assert N.lib.pasif_batch_forward(None, None, 1.0, 0, 1, None, None) == N.ERR_INVALID
     assert N.lib.pasif_driver_allocate_system(None) == N.ERR_INVALID
+    assert N.lib.pasif_batch_reserve(None, 1, 1) == N.ERR_INVALID
+    assert N.lib.pasif_batch_set_adjoint_storage(None, 0) == N.ERR_INVALID
+    assert N.lib.pasif_batch_adjoint(None, None, 1.0, 1, None, None, None, None, None, 0, None) == N.ERR_INVALID
+    rid, n = C.c_int(), C.c_int()
+    assert N.lib.pasif_pool_admit(None, 1, None, None, None, None, 1, 1, 1, 0, 0, C.byref(rid)) == N.ERR_INVALID
+    assert N.lib.pasif_pool_launch(None) == N.ERR_INVALID
+    assert N.lib.pasif_pool_poll(None, None, 0, C.byref(n)) == N.ERR_INVALID
+    assert N.lib.pasif_pool_harvest(None, 0, None, None, None) == N.ERR_INVALID
+    assert "null" in N.last_error()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32", "fp32_kahan"])

@@ -307,14 +307,24 @@ int pasif_forward(const pasif_pattern* pattern, int precision, int n_sys, const 
  * DEVICE pointer: values[n_sys][P], x0[n_sys][n], exc_index[n_sys],
  * signals[n_exc][len], im[2*window] (window 0: sample and hold),
  * state_out[n_sys][n].  Work space: a 32 MiB array owned by the library on
- * every GPU that loads it (until exit); 8*n_sys*(P+7n) bytes must fit in
- * 31 MiB and the pattern in 1 MiB, else PASIF_ERR_INVALID.  The first call on
- * a device looks up the array's address (make it before any stream
+ * every GPU that loads it (until exit); 8*n_sys*(P+7n) + 4*n_sys bytes must
+ * fit in 31 MiB and the pattern in 1 MiB, else PASIF_ERR_INVALID.  The first
+ * call on a device looks up the array's address (make it before any stream
  * capture).  Calls share the array and keep its last contents: calls whose
- * GPU work overlaps race.  Returns once the work is queued on `stream`. */
+ * GPU work overlaps race.  Returns once the work is queued on `stream`; it
+ * neither allocates nor waits for the device (the pattern is passed as kernel
+ * arguments).  The excitation indices are checked on the device: a system
+ * whose index lies outside [0, n_exc) reads no signal, its state_out row is
+ * NaN, and pasif_forward_noalloc_status reports it. */
 int pasif_forward_noalloc(const pasif_pattern* pattern, int n_sys, const double* values, const double* x0,
                           const int* exc_index, const double* signals, int n_exc, int len, int window,
                           const double* im, double h, int step0, int nsteps, double* state_out, void* stream);
+/* Status of the last pasif_forward_noalloc call on the current device, read
+ * from the library's array after waiting for `stream` (pass the stream of
+ * that call): *n_bad = systems with an out-of-range excitation index,
+ * *first_bad = the lowest of them (n_sys when none; may be NULL).  No
+ * counterpart in the reference. */
+int pasif_forward_noalloc_status(int* n_bad, int* first_bad, void* stream);
 
 #ifdef __cplusplus
 }

@@ -132,6 +132,7 @@ _SIGS = {
     "pasif_fma_peak": (C.c_int, [C.c_int, _dp]),
     "pasif_forward_noalloc": (C.c_int, [C.POINTER(PatternC), C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int,
                                         _vp, C.c_double, C.c_int, C.c_int, _vp, _vp]),
+    "pasif_forward_noalloc_status": (C.c_int, [_ip, _ip, _vp]),
     "pasif_forward": (C.c_int, [C.POINTER(PatternC), C.c_int, C.c_int, _dp, _dp, _ip, _dp, C.c_int, C.c_int,
                                 C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.POINTER(ReducersC), _dp, _dp, _dp]),
 }

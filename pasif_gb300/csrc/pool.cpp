@@ -229,6 +229,7 @@ int Pool::admit(int n_sys, const double* values, const double* x0, const int* ex
                 int n_exc, int len, int nsteps, int max_start, int sq_start, int* req_id, std::string* err) {
     const Pattern& pat = plan_->pat;
     const int n = pat.n, P = pat.P();
+    if (failed_) { *err = "pool unusable after a failed admission (its device state is unknown)"; return 2; }
     if (n_sys < 1 || n_exc < 1 || len < 1 || nsteps < 0 || !values || !x0 || !exc_index || !signals) {
         *err = "bad request";
         return 1;
@@ -317,9 +318,11 @@ int Pool::admit(int n_sys, const double* values, const double* x0, const int* ex
         PL_CUDA(cudaStreamSynchronize(st_), "cudaStreamSynchronize");   // staging reused by the next admission
         return 0;
     };
-    if (const int rc = stage()) {   // the slots and the arena space go back to the pool
-        for (auto it = r.slots.rbegin(); it != r.slots.rend(); ++it) free_.push_back(*it);
-        arena_free(off, table);
+    if (const int rc = stage()) {
+        // part of the upload may have run (the `remain` scatter is queued
+        // last, but a failed stream synchronisation leaves it unknown whether
+        // it ran): the slots cannot be handed out again, nor the pool trusted
+        failed_ = true;
         return rc;
     }
     *req_id = next_id_++;
@@ -328,6 +331,7 @@ int Pool::admit(int n_sys, const double* values, const double* x0, const int* ex
 }
 
 int Pool::launch(std::string* err) {
+    if (failed_) { *err = "pool unusable after a failed admission (its device state is unknown)"; return 2; }
     if (reqs_.empty()) return 0;
     PL_CUDA(cudaGraphLaunch(graph_, st_), "cudaGraphLaunch");
     return 0;

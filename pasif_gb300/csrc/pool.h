@@ -68,6 +68,10 @@ private:
     std::map<long long, long long> holes_;  // arena free list: offset -> size
     std::map<int, PoolRequest> reqs_;
     int next_id_ = 1;
+    // set when an admission failed after part of its upload was queued: the
+    // device-side slot records may then be inconsistent (a slot may read as
+    // busy with a stale request), so the pool refuses every further call
+    bool failed_ = false;
     JitKernel k_;
     cudaStream_t st_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;

@@ -329,10 +329,15 @@ class Server:
         with self._cv:
             self._results[req.rid] = res
             self._outstanding += 1
+        if req.kind in ("forward", "adjoint") and req.cls not in self.specs:
+            return self._finish(res, error=f"unknown request class {req.cls!r}")
         if req.kind == "forward":
             if n_sys > self.capacity or table > self.arena_samples:
                 return self._finish(res, error="request larger than a serving pool (slots or signal arena)")
-            self._pool(req.cls)
+            try:
+                self._pool(req.cls)
+            except Exception as exc:   # pool creation failed: this request fails, the server goes on
+                return self._finish(res, error=f"serving pool for class {req.cls!r} unavailable: {exc}")
             with self._cv:
                 self._fwd_q[req.cls].append((req, res))
                 self._cv.notify_all()

@@ -120,6 +120,34 @@ def test_invalid_forward_request_fails_alone():
     assert res[0].error is None and res[2].error is None
     np.testing.assert_array_equal(res[2].state, np.full((3, 2), 4.0))
 
+def test_unknown_class_or_failing_pool_fails_the_request():
+    """A request of a class the server does not serve, or whose pool cannot be
+    made, gets an error result at once: wait() does not wait for it."""
+    srv, _ = make_server()
+    srv.start()
+    for kind in ("forward", "adjoint"):
+        r = req(0 if kind == "forward" else 1, kind, 2)
+        r.cls = "no such class"
+        srv.submit(r)
+    srv.submit(req(2, "forward", 2))
+    assert srv.wait(5.0)
+    res = srv.results()
+    assert "unknown request class" in res[0].error and "unknown request class" in res[1].error
+    assert res[2].error is None
+    srv.stop()
+
+    def broken(spec):
+        raise RuntimeError("kernel build failed")
+    srv = S.Server({"a": S.ClassSpec(PAT, 0.01, 0, None, (0,), chunk=10)}, capacity=8, arena_samples=1000,
+                   adjoint_budget=100, adjoint_workers=1, pool_factory=broken,
+                   adjoint_runner=lambda sp, rq, st: (rq.values, rq.x0), stream_factory=lambda prio: None)
+    srv.start()
+    srv.submit(req(5, "forward", 2))
+    assert srv.wait(5.0)
+    assert "unavailable" in srv.results()[5].error
+    srv.stop()
+
+
 def test_adjoint_budget():
     lock, state = threading.Lock(), {"now": 0, "peak": 0}
     need = S.adjoint_bytes(PAT, 4, 25, 10, "fp32_kahan")

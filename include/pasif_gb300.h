@@ -37,6 +37,12 @@ extern "C" {
 #define PASIF_FP64 0            /* reference precision (reel = double)     */
 #define PASIF_FP32 1            /* reel = float                            */
 #define PASIF_FP32_KAHAN 2      /* FP32 stages, compensated state update   */
+#define PASIF_FP32_EXT 3        /* FP32 stages; state (and adjoint state)
+                                   as double-float pairs; the FP64 values'
+                                   FP32 residuals and the exact h/6 applied
+                                   once per step: long-horizon precision
+                                   mode (pattern-specialised kernels only;
+                                   not for serving pools)                  */
 
 #define PASIF_HOST 0            /* pointers are host memory                */
 #define PASIF_DEVICE 1          /* pointers are device memory (current GPU) */

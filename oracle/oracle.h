@@ -69,7 +69,9 @@ typedef struct orc_red {
 
 /* Integrate one instance (one system driven by excitation row e) from x0 for
  * nsteps steps starting at step index step0.  mode: 0 plain, 1 Kahan update
- * (the Kahan mode only differs in the float build).  Outputs (any may be NULL):
+ * (the Kahan mode only differs in the float build), 2 extended state (float
+ * build: double-float state, FP32 residuals of the values applied once per
+ * step, h/6 as h6 + h6lo; the output state is hi + lo).  Outputs (any may be NULL):
  * out_state[n], out_max[n_max], out_sq[1]. */
 void orc_integrate_d(const orc_sys* s, const double* x0, int e, const orc_exc* ex,
                      double h, int step0, int nsteps, int mode, const orc_red* red,

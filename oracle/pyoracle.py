@@ -121,7 +121,7 @@ def make_red(max_comp=(), max_start=0, sq_comp=(), sq_start=0):
 def batch_forward(pattern, values, x0, exc_index, x, h, nsteps, window=0, im=None, precision="fp64", step0=0,
                   max_comp=(), max_start=0, sq_comp=(), sq_start=0, threads=0):
     """Oracle of pasif_gb300.batch: returns (state, max, sq).
-    precision: "fp64", "fp32" or "fp32_kahan" (float build of the oracle)."""
+    precision: "fp64", "fp32", "fp32_kahan" or "fp32_ext" (float build of the oracle)."""
     v = _d(values).reshape(-1, pattern.P)
     B = v.shape[0]
     x0 = _d(x0).reshape(B, pattern.n)
@@ -133,7 +133,7 @@ def batch_forward(pattern, values, x0, exc_index, x, h, nsteps, window=0, im=Non
     mx = np.empty((B, max(red.n_max, 1)))
     sq = np.empty(B)
     f = lib.orc_batch_forward_d if precision == "fp64" else lib.orc_batch_forward_f
-    mode = 1 if precision == "fp32_kahan" else 0
+    mode = {"fp32_kahan": 1, "fp32_ext": 2}.get(precision, 0)
     f(C.byref(s), B, v.ctypes.data_as(_dp), x0.ctypes.data_as(_dp), e.ctypes.data_as(_ip), C.byref(ex), float(h),
       int(step0), int(nsteps), mode, C.byref(red), st.ctypes.data_as(_dp), mx.ctypes.data_as(_dp),
       sq.ctypes.data_as(_dp), int(threads))

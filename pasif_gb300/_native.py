@@ -22,7 +22,7 @@ ERR_MEMORY = 4
 ERR_STATE = 5
 ERR_LENGTH = 6
 
-FP64, FP32, FP32_KAHAN = 0, 1, 2
+FP64, FP32, FP32_KAHAN, FP32_EXT = 0, 1, 2, 3
 HOST, DEVICE = 0, 1
 KERNEL_NONE, KERNEL_GENERIC, KERNEL_SPECIALISED = 0, 1, 2
 PLAN_GENERIC_ONLY = 1
@@ -30,7 +30,7 @@ PLAN_NO_LITERALS = 2
 PLAN_WARP_SLICED = 4
 PLAN_NO_WARP_SLICED = 8
 
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32_kahan": FP32_KAHAN}
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32_kahan": FP32_KAHAN, "fp32_ext": FP32_EXT}
 
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)

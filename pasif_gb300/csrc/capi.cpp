@@ -543,34 +543,18 @@ int pasif_plan_jit_report_pool(const pasif_plan* p, int window, const double* im
     });
 }
 
-static pasif::Literals literals_of(const pasif::Pattern& pat, bool f32, const double* values, int n_sys) {
-    const int P = pat.P();
-    pasif::Literals lit;
-    lit.is_lit.assign(P, 0);
-    lit.value.assign(P, 0.0);
-    if (values && n_sys > 0)
-        for (int q = 0; q < P; ++q) {
-            bool same = true;
-            const double v0 = f32 ? (double)(float)values[q] : values[q];
-            for (int b = 1; b < n_sys && same; ++b) {
-                const double v = f32 ? (double)(float)values[(long long)b * P + q] : values[(long long)b * P + q];
-                same = v == v0 && std::signbit(v) == std::signbit(v0);
-            }
-            lit.is_lit[q] = same && std::isfinite(v0);
-            lit.value[q] = v0;
-        }
-    return lit;
-}
-
 int pasif_plan_jit_report_adjoint(const pasif_plan* p, const double* values, int n_sys, unsigned long long sq_mask,
                                   char* log, long long capacity, long long* out_len) {
     if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null plan");
     return guard([&] {
         const bool f32 = p->p->precision != pasif::kFP64;
         const std::string src =
-            pasif::adj_source(p->p->pat, literals_of(p->p->pat, f32, values, n_sys), f32, sq_mask,
-                              p->p->slicing < 0 ? 0 : pasif::ws_slices_adjoint(p->p->pat, f32, p->p->slicing > 0),
-                              p->p->precision == pasif::kFP32Kahan);
+            pasif::adj_source(p->p->pat, pasif::literals_of(p->p->pat, p->p->precision, values, n_sys), f32, sq_mask,
+                              p->p->slicing < 0 ? 0
+                                                : pasif::ws_slices_adjoint(p->p->pat, f32, p->p->slicing > 0,
+                                                                           p->p->precision == pasif::kFP32Ext),
+                              p->p->precision == pasif::kFP32Kahan || p->p->precision == pasif::kFP32Ext,
+                              p->p->precision == pasif::kFP32Ext);
         std::string report, err;
         if (!pasif::compile_report(src, &report, &err)) return fail(PASIF_ERR_NVRTC, err);
         report += "\n// ---- source ----\n" + src;
@@ -603,28 +587,15 @@ int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys, 
     if (!p || !p->p) return fail(PASIF_ERR_INVALID, "null plan");
     return guard([&] {
         const pasif::Pattern& pat = p->p->pat;
-        const int P = pat.P();
         const bool f32 = p->p->precision != pasif::kFP64;
-        pasif::Literals lit;
-        lit.is_lit.assign(P, 0);
-        lit.value.assign(P, 0.0);
-        if (values && n_sys > 0)
-            for (int q = 0; q < P; ++q) {
-                bool same = true;
-                const double v0 = f32 ? (double)(float)values[q] : values[q];
-                for (int b = 1; b < n_sys && same; ++b) {
-                    const double v = f32 ? (double)(float)values[(long long)b * P + q] : values[(long long)b * P + q];
-                    same = v == v0 && std::signbit(v) == std::signbit(v0);
-                }
-                lit.is_lit[q] = same && std::isfinite(v0);
-                lit.value[q] = v0;
-            }
+        const pasif::Literals lit = pasif::literals_of(pat, p->p->precision, values, n_sys);
         pasif::FwdKernelKey key;
         key.f32 = f32;
-        key.kahan = p->p->precision == pasif::kFP32Kahan;
+        key.kahan = p->p->precision == pasif::kFP32Kahan || p->p->precision == pasif::kFP32Ext;
+        key.ext = p->p->precision == pasif::kFP32Ext;
         key.max_mask = max_mask;
         key.sq_mask = sq_mask;
-        key.slices = p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0, n_sys);
+        key.slices = p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0, n_sys, key.ext);
         if (window < 0 || (window > 0 && (!im || (window & (window - 1)))))
             return fail(PASIF_ERR_INVALID, "window must be 0 or a power of two with weights");
         key.window = window;

@@ -229,7 +229,7 @@ int Driver::load_excitations(const double* const* sig, const long long* len, int
 }
 
 int Driver::set_precision(int p, std::string* err) {
-    if (p < kFP64 || p > kFP32Kahan) { *err = "unknown precision"; return 1; }
+    if (p < kFP64 || p > kFP32Ext) { *err = "unknown precision"; return 1; }
     if (p != precision_) { precision_ = p; signals_.reset(); groups_.clear(); }
     return 0;
 }

@@ -87,6 +87,48 @@ static int upload_interleaved(const double* src, int B, int k, bool f32, int mem
     return 0;
 }
 
+// [B][k] double (host or device) -> [2k][B] FP32: the high parts (v rounded
+// to FP32) of the k values, then their low parts (v minus its high part,
+// rounded to FP32); the extended-state mode's layout of values and x0.
+static int upload_split(const double* src, int B, int k, int memory, DevBuf& dst, DevBuf& split, DevBuf& stage,
+                        cudaStream_t st, std::string* err) {
+    const long long total = (long long)B * k;
+    PK_CUDA(dst.ensure((size_t)(total > 0 ? 2 * total : 1) * sizeof(float)), "cudaMalloc");
+    if (total == 0) return 0;
+    const double* dsrc = src;
+    if (memory == kHost) {
+        PK_CUDA(stage.ensure((size_t)total * sizeof(double)), "cudaMalloc");
+        PK_CUDA(cudaMemcpyAsync(stage.p, src, (size_t)total * sizeof(double), cudaMemcpyHostToDevice, st),
+                "cudaMemcpyAsync");
+        dsrc = stage.as<double>();
+    }
+    PK_CUDA(split.ensure((size_t)total * 2 * sizeof(double)), "cudaMalloc");
+    PK_CUDA(pk::launch_split_hi_lo(dsrc, split.as<double>(), B, k, st), "split kernel");
+    PK_CUDA(pk::launch_to_interleaved(split.as<double>(), dst.p, B, 2 * k, true, st), "layout kernel");
+    return 0;
+}
+
+// [k][B] FP32 high and low parts -> [B][k] double hi + lo (host or device).
+static int download_pair(const void* hi, const void* lo, int B, int k, double scale, double* out, int memory,
+                         DevBuf& stage, cudaStream_t st, std::string* err) {
+    const long long total = (long long)B * k;
+    if (total == 0 || !out) return 0;
+    double* ddst = out;
+    if (memory == kHost) {
+        PK_CUDA(stage.ensure((size_t)total * sizeof(double)), "cudaMalloc");
+        ddst = stage.as<double>();
+    }
+    PK_CUDA(pk::launch_from_interleaved_pair(static_cast<const float*>(hi), static_cast<const float*>(lo), ddst, B, k,
+                                             scale, st),
+            "layout kernel");
+    if (memory == kHost) {
+        PK_CUDA(cudaMemcpyAsync(out, ddst, (size_t)total * sizeof(double), cudaMemcpyDeviceToHost, st),
+                "cudaMemcpyAsync");
+        PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    }
+    return 0;
+}
+
 // [k][B] (compute precision or double) -> [B][k] double (host or device).
 static int download_interleaved(const void* src, int B, int k, bool f32, double scale, double* out, int memory,
                                 DevBuf& stage, cudaStream_t st, std::string* err) {
@@ -156,11 +198,13 @@ int Batch::reserve(int n_sys, int nsteps, std::string* err) {
     const size_t Bn = (size_t)(n_sys > 0 ? n_sys : 1), wide = std::max(P, n);
     const size_t C = nsteps > 0 ? (size_t)std::ceil(std::sqrt((double)nsteps)) : 1;
     const size_t nck = nsteps > 0 ? ((size_t)nsteps + C - 1) / C : 1;
-    PK_CUDA(vals.ensure(Bn * P * rs), "cudaMalloc");
-    PK_CUDA(x0.ensure(Bn * n * rs), "cudaMalloc");
+    const size_t np = parts();   // kFP32Ext: high and low parts
+    PK_CUDA(vals.ensure(Bn * P * np * rs), "cudaMalloc");
+    PK_CUDA(x0.ensure(Bn * n * np * rs), "cudaMalloc");
     PK_CUDA(stage.ensure(Bn * wide * sizeof(double)), "cudaMalloc");
+    if (ext()) PK_CUDA(split.ensure(Bn * wide * 2 * sizeof(double)), "cudaMalloc");
     PK_CUDA(exc.ensure(Bn * sizeof(int)), "cudaMalloc");
-    PK_CUDA(state.ensure(Bn * n * rs), "cudaMalloc");
+    PK_CUDA(state.ensure(Bn * n * np * rs), "cudaMalloc");
     PK_CUDA(out_max.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(out_sq.ensure(Bn * rs), "cudaMalloc");
     PK_CUDA(ckpt.ensure(Bn * 2 * n * nck * rs), "cudaMalloc");
@@ -207,13 +251,46 @@ int plan_create(const Pattern& pat, int precision, bool generic_only, std::share
                 std::string* err) {
     std::string v = pat.validate();
     if (!v.empty()) { *err = v; return 1; }
-    if (precision < kFP64 || precision > kFP32Kahan) { *err = "unknown precision"; return 1; }
+    if (precision < kFP64 || precision > kFP32Ext) { *err = "unknown precision"; return 1; }
+    if (precision == kFP32Ext && generic_only) {
+        *err = "the extended-state precision runs on the pattern-specialised kernels only";
+        return 1;
+    }
     auto p = std::make_shared<Plan>();
     p->pat = pat;
     p->precision = precision;
     p->generic_only = generic_only;
     *out = p;
     return 0;
+}
+
+Literals literals_of(const Pattern& pat, int precision, const double* values, int n_sys) {
+    const int P = pat.P();
+    Literals lit;
+    lit.is_lit.assign(P, 0);
+    lit.value.assign(P, 0.0);
+    lit.is_lit_lo.assign(P, 0);
+    lit.value_lo.assign(P, 0.0);
+    if (precision < 0 || !values || n_sys <= 0) return lit;
+    const bool f = precision != kFP64;
+    auto hi_of = [&](double v) { return f ? (double)(float)v : v; };
+    auto lo_of = [](double v) { return (double)(float)(v - (double)(float)v); };   // kFP32Ext low part
+    auto same_bits = [](double a, double b) { return std::memcmp(&a, &b, sizeof(double)) == 0; };
+    for (int q = 0; q < P; ++q) {
+        const double v0 = hi_of(values[q]);
+        bool same = true;
+        for (int b = 1; b < n_sys && same; ++b) same = same_bits(hi_of(values[(long long)b * P + q]), v0);
+        lit.value[q] = v0;
+        lit.is_lit[q] = same && std::isfinite(v0) ? 1 : 0;
+        if (precision == kFP32Ext) {
+            const double l0 = lo_of(values[q]);
+            bool same_lo = true;
+            for (int b = 1; b < n_sys && same_lo; ++b) same_lo = same_bits(lo_of(values[(long long)b * P + q]), l0);
+            lit.value_lo[q] = l0;
+            lit.is_lit_lo[q] = same_lo && std::isfinite(l0) ? 1 : 0;
+        }
+    }
+    return lit;
 }
 
 int Plan::ensure_device(std::string* err) {
@@ -241,9 +318,11 @@ int Batch::set(const double* values, const double* x0h, const int* exc_index, in
     const bool f = f32();
     if (B > 0 && ((P > 0 && !values) || !x0h || !exc_index)) { *err = "null input array"; return 1; }
     if (int rc0 = plan->ensure_device(err)) return rc0;
-    int rc = upload_interleaved(values, B, P, f, memory, vals, stage, st, err);
+    int rc = ext() ? upload_split(values, B, P, memory, vals, split, stage, st, err)
+                   : upload_interleaved(values, B, P, f, memory, vals, stage, st, err);
     if (rc) return rc;
-    rc = upload_interleaved(x0h, B, n, f, memory, x0, stage, st, err);
+    rc = ext() ? upload_split(x0h, B, n, memory, x0, split, stage, st, err)
+               : upload_interleaved(x0h, B, n, f, memory, x0, stage, st, err);
     if (rc) return rc;
     PK_CUDA(exc.ensure((size_t)(B > 0 ? B : 1) * sizeof(int)), "cudaMalloc");
     std::vector<int> idx(B);
@@ -258,27 +337,7 @@ int Batch::set(const double* values, const double* x0h, const int* exc_index, in
         if (idx[i] > max_exc_) max_exc_ = idx[i];
     }
     // values shared by every instance become compile-time constants
-    lit.is_lit.assign(P, 0);
-    lit.value.assign(P, 0.0);
-    if (memory == kHost && B > 0 && !plan->no_literals) {
-        for (int q = 0; q < P; ++q) {
-            bool same = true;
-            if (f) {
-                const float v0 = (float)values[q];
-                for (int b = 1; b < B && same; ++b) {
-                    const float v = (float)values[(long long)b * P + q];
-                    same = std::memcmp(&v, &v0, sizeof(float)) == 0;
-                }
-                lit.value[q] = (double)v0;
-            } else {
-                const double v0 = values[q];
-                for (int b = 1; b < B && same; ++b)
-                    same = std::memcmp(&values[(long long)b * P + q], &v0, sizeof(double)) == 0;
-                lit.value[q] = v0;
-            }
-            lit.is_lit[q] = same && std::isfinite(lit.value[q]) ? 1 : 0;
-        }
-    }
+    lit = literals_of(pat, memory == kHost && !plan->no_literals ? plan->precision : -1, values, B);
     PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     inputs_set = true;
     return 0;
@@ -317,6 +376,7 @@ static void fill_fwd(pk::FwdArgs<R>& a, Batch& bt, const Signals& sig, double h,
     a.h = (R)h;
     a.h2 = (R)(h / 2.0);
     a.h6 = (R)(h / 6.0);
+    a.h6lo = (R)(h / 6.0 - (double)(R)(h / 6.0));
     a.B = bt.B;
     a.step0 = (unsigned)step0;
     a.nsteps = nsteps;
@@ -356,7 +416,8 @@ bool Batch::fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long 
     const bool f = f32();
     FwdKernelKey key;
     key.f32 = f;
-    key.kahan = plan->precision == kFP32Kahan;
+    key.kahan = compensated();
+    key.ext = ext();
     key.max_mask = mm;
     key.sq_mask = sm;
     key.traj = traj_mode;
@@ -364,14 +425,14 @@ bool Batch::fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long 
     key.window = (int)sig.w;
     key.wn.assign(sig.im_host.begin(), sig.im_host.begin() + sig.w);
     key.wc.assign(sig.im_host.begin() + sig.w, sig.im_host.end());
-    key.slices = plan->slicing < 0 ? 0 : ws_slices(pat, f, plan->slicing > 0, B);
+    key.slices = plan->slicing < 0 ? 0 : ws_slices(pat, f, plan->slicing > 0, B, ext());
     return get_fwd_kernel(pat, lit, key, k, jerr);
 }
 
 cudaError_t Batch::launch_fwd_jit(const JitKernel& k, const Signals& sig, double h, int step0, int nsteps,
                                   const Reducers& red, unsigned long long mm, unsigned long long sm, int traj_every,
                                   long long traj_slots, void* state_p, void* traj_p, cudaStream_t st,
-                                  const void* comp_p) {
+                                  const void* comp_p, void* comp_out_p) {
     const dim3 grid((unsigned)((B + k.per_block - 1) / k.per_block));
     if (f32()) {
         pk::FwdArgs<float> a;
@@ -379,6 +440,7 @@ cudaError_t Batch::launch_fwd_jit(const JitKernel& k, const Signals& sig, double
         a.state = static_cast<float*>(state_p);
         a.traj = static_cast<float*>(traj_p);
         a.comp = static_cast<const float*>(comp_p);
+        a.comp_out = static_cast<float*>(comp_out_p);
         void* args[] = {&a};
         return cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
     }
@@ -387,6 +449,7 @@ cudaError_t Batch::launch_fwd_jit(const JitKernel& k, const Signals& sig, double
     a.state = static_cast<double*>(state_p);
     a.traj = static_cast<double*>(traj_p);
     a.comp = static_cast<const double*>(comp_p);
+    a.comp_out = static_cast<double*>(comp_out_p);
     void* args[] = {&a};
     return cudaLaunchKernel((const void*)k.fn, grid, dim3(k.block), args, (size_t)k.smem, st);
 }
@@ -409,24 +472,31 @@ int Batch::forward(const Signals& sig, double h, int step0, int nsteps, const Re
     last_h = h;
     const size_t rs = rsize();
     const size_t Bn = (size_t)(B > 0 ? B : 1);
-    PK_CUDA(state.ensure(Bn * (size_t)n * rs), "cudaMalloc");
+    PK_CUDA(state.ensure(Bn * (size_t)n * parts() * rs), "cudaMalloc");   // kFP32Ext: high, then low parts
     PK_CUDA(out_max.ensure(Bn * (size_t)(n_max > 0 ? n_max : 1) * rs), "cudaMalloc");
     PK_CUDA(out_sq.ensure(Bn * rs), "cudaMalloc");
     if (traj_every > 0) PK_CUDA(traj.ensure(Bn * (size_t)n * (size_t)(traj_slots > 0 ? traj_slots : 1) * rs), "cudaMalloc");
     if (B == 0) { last_kind = kNone; return 0; }
-    PK_CUDA(cudaMemcpyAsync(state.p, x0.p, (size_t)B * n * rs, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
+    PK_CUDA(cudaMemcpyAsync(state.p, x0.p, (size_t)B * n * parts() * rs, cudaMemcpyDeviceToDevice, st),
+            "cudaMemcpyAsync");
     const bool kahan = plan->precision == kFP32Kahan;
     JitKernel k;
     std::string jerr;
     if (fwd_kernel(sig, mm, sm, traj_every > 0 ? 1 : 0, &k, &jerr)) {
+        // kFP32Ext: the low parts of the state follow the high parts in `state`, read and written in place
+        char* lo = ext() ? state.as<char>() + (size_t)B * n * rs : nullptr;
         PK_CUDA(launch_fwd_jit(k, sig, h, step0, nsteps, red, mm, sm, traj_every, traj_slots, state.p,
-                               traj_every > 0 ? traj.p : nullptr, st),
+                               traj_every > 0 ? traj.p : nullptr, st, lo, lo),
                 "specialised forward kernel launch");
         last_kind = kSpecialised;
         last_jit = k;
         return 0;
     }
     if (!plan->generic_only) last_jit_error = jerr;
+    if (ext()) {
+        *err = "the extended-state precision needs the pattern-specialised kernel: " + jerr;
+        return 3;
+    }
     PK_CUDA(scratch.ensure(Bn * 6 * (size_t)n * rs), "cudaMalloc");
     cudaError_t e;
     if (f) {
@@ -447,7 +517,9 @@ int Batch::get(double* state_out, double* max_out, double* sq_out, double h, int
                std::string* err) {
     const int n = plan->pat.n;
     const bool f = f32();
-    int rc = download_interleaved(state.p, B, n, f, 1.0, state_out, memory, stage, st, err);
+    int rc = ext() ? download_pair(state.p, state.as<char>() + (size_t)B * n * rsize(), B, n, 1.0, state_out, memory,
+                                   stage, st, err)
+                   : download_interleaved(state.p, B, n, f, 1.0, state_out, memory, stage, st, err);
     if (rc) return rc;
     if (max_out && n_max > 0) {
         rc = download_interleaved(out_max.p, B, n_max, f, 1.0, max_out, memory, stage, st, err);
@@ -498,10 +570,16 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     const size_t Bn = (size_t)B;
     JitKernel jk;
     std::string jerr;
-    const int slices = plan->slicing < 0 ? 0 : ws_slices_adjoint(pat, f, plan->slicing > 0);
+    const int slices = plan->slicing < 0 ? 0 : ws_slices_adjoint(pat, f, plan->slicing > 0, ext());
     const bool jit = !plan->generic_only &&
-                     get_adj_kernel(pat, lit, f, plan->precision == kFP32Kahan, g_sq ? sm : 0ull, slices, &jk, &jerr);
+                     get_adj_kernel(pat, lit, f, compensated(), g_sq ? sm : 0ull, slices, &jk, &jerr, ext());
     if (!jit && !plan->generic_only) last_jit_error = jerr;
+    if (!jit && ext()) {
+        *err = "the extended-state precision needs the pattern-specialised adjoint kernel: " + jerr;
+        return 3;
+    }
+    // kFP32Ext: the low parts of x0 (start of the forward passes)
+    const char* x0lo = ext() ? x0.as<char>() + (size_t)B * n * rs : nullptr;
     // The trajectory the backward sweep reads, in one of three ways (same bits):
     //  stored   (within adj_store_limit): the batch's forward kernel writes
     //           every step's slot once;
@@ -541,12 +619,12 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     }
     if (stored) {   // the forward kernel's state runs in dx0 (replaced by the adjoint later)
         PK_CUDA(cudaMemcpyAsync(dx0.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
-        PK_CUDA(launch_fwd_jit(fk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, 1, nsteps, dx0.p, buf.p, st),
+        PK_CUDA(launch_fwd_jit(fk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, 1, nsteps, dx0.p, buf.p, st, x0lo),
                 "trajectory forward kernel launch");
     }
     if (replayed) {   // checkpoints of state and compensation every C steps
         PK_CUDA(cudaMemcpyAsync(adj_state.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
-        PK_CUDA(launch_fwd_jit(ckk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, C, nck, adj_state.p, ckpt.p, st),
+        PK_CUDA(launch_fwd_jit(ckk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, C, nck, adj_state.p, ckpt.p, st, x0lo),
                 "checkpoint forward kernel launch");
     }
     cudaError_t e;
@@ -572,12 +650,14 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     a.nsteps = nsteps;                                                \
     a.C = C;                                                          \
     a.nck = nck;                                                      \
-    a.kahan = plan->precision == kFP32Kahan ? 1 : 0;                  \
+    a.kahan = compensated() ? 1 : 0;                                  \
+    a.ext = ext() ? 1 : 0;                                            \
+    a.h6lo = (R_)(h / 6.0 - (double)(R_)(h / 6.0));                   \
     a.sq_start = red.sq_start;                                        \
     a.sq_mask = g_sq ? sm : 0ull;                                     \
     a.stored = stored || replayed ? 1 : 0;
     const dim3 grid((unsigned)(jit ? (B + jk.per_block - 1) / jk.per_block : (B + 127) / 128));
-    if (jit && plan->precision == kFP32Kahan) PK_CUDA(lamc.ensure(Bn * (size_t)n * rs), "cudaMalloc");
+    if (jit && compensated()) PK_CUDA(lamc.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     // Specialised kernels over many blocks: forward segments and backward chunk
     // groups of about kAdjLaunchSteps·16/n steps each, so that a launch lasts
     // milliseconds and work on other streams (serving chunks, small adjoints) is
@@ -643,7 +723,8 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     PK_CUDA(e, "adjoint kernel launch");
     int rc = download_interleaved(pbar.p, B, P, false, 1.0, d_values, memory, adj_stage, st, err);
     if (rc) return rc;
-    rc = download_interleaved(dx0.p, B, n, f, 1.0, d_x0, memory, adj_stage, st, err);
+    rc = ext() ? download_pair(dx0.p, lamc.p, B, n, 1.0, d_x0, memory, adj_stage, st, err)   // high + low parts
+               : download_interleaved(dx0.p, B, n, f, 1.0, d_x0, memory, adj_stage, st, err);
     if (rc) return rc;
     PK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     return 0;

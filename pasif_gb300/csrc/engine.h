@@ -13,7 +13,12 @@
 
 namespace pasif {
 
-enum Precision { kFP64 = 0, kFP32 = 1, kFP32Kahan = 2 };
+// kFP32Ext: FP32 stages, state and adjoint state as double-float pairs (hi +
+// lo), the FP64 values split into FP32 high parts (stages) and low parts (a
+// once-per-step residual term), h/6 carried as h6 + h6lo: the precision mode
+// for long horizons, where FP32 rounding of the values and of h/6 acts as a
+// systematic perturbation of the system.  Pattern-specialised kernels only.
+enum Precision { kFP64 = 0, kFP32 = 1, kFP32Kahan = 2, kFP32Ext = 3 };
 enum Memory { kHost = 0, kDevice = 1 };
 enum KernelKind { kNone = 0, kGeneric = 1, kSpecialised = 2 };
 
@@ -86,6 +91,11 @@ struct Plan {
 int plan_create(const Pattern& pat, int precision, bool generic_only, std::shared_ptr<Plan>* out,
                 std::string* err);
 
+// Values shared by every instance (host values[n_sys][P]) as compile-time
+// constants of the specialised kernels, in the compute precision of
+// `precision`; kFP32Ext also the low parts.  No values: no literals.
+Literals literals_of(const Pattern& pat, int precision, const double* values, int n_sys);
+
 struct Reducers {
     std::vector<int> max_comp;   // ascending, < 64
     int max_start = 0;
@@ -99,6 +109,7 @@ struct Batch {
     int B = 0;
     DevBuf vals, x0, state, exc, out_max, out_sq, scratch, stage, traj;
     DevBuf ckpt, buf, pbar, dx0, gfin, gsq, adj_stage, lamc, adj_state;
+    DevBuf split;                 // kFP32Ext: values / x0 split into high and low parts (device inputs)
     Literals lit;
     int n_max = 0;
     bool has_sq = false;
@@ -122,6 +133,11 @@ struct Batch {
     }
 
     bool f32() const { return plan->precision != kFP64; }
+    bool ext() const { return plan->precision == kFP32Ext; }
+    // compensated update (Kahan, or the double-float state of kFP32Ext)
+    bool compensated() const { return plan->precision == kFP32Kahan || ext(); }
+    // vectors per state-sized buffer (values, x0, state): high and low parts in kFP32Ext
+    size_t parts() const { return ext() ? 2 : 1; }
     size_t rsize() const { return f32() ? sizeof(float) : sizeof(double); }
     // The specialised forward kernel for these reducers (false: none, *jerr why).
     // traj_mode: 0 none, 1 states every traj_every steps, 2 the adjoint trajectory.
@@ -133,7 +149,7 @@ struct Batch {
     cudaError_t launch_fwd_jit(const JitKernel& k, const Signals& sig, double h, int step0, int nsteps,
                                const Reducers& red, unsigned long long mm, unsigned long long sm, int traj_every,
                                long long traj_slots, void* state_p, void* traj_p, cudaStream_t st,
-                               const void* comp_p = nullptr);
+                               const void* comp_p = nullptr, void* comp_out_p = nullptr);
 
     // New instance count; the device buffers are kept and grown by the next
     // set / solve when needed (a batch reused for requests of any size).

@@ -109,6 +109,26 @@ __global__ void from_interleaved(const R* __restrict__ src, double* __restrict__
     dst[t] = (double)src[p * B + b] * scale;
 }
 
+__global__ void split_hi_lo(const double* __restrict__ src, double* __restrict__ dst, int B, int k) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)B * k;
+    if (t >= total) return;
+    const long long b = t / k, p = t % k;
+    const double v = src[t];
+    const double hi = (double)(float)v;
+    dst[b * 2 * k + p] = hi;
+    dst[b * 2 * k + k + p] = v - hi;   // exact in double
+}
+
+__global__ void from_interleaved_pair(const float* __restrict__ hi, const float* __restrict__ lo,
+                                      double* __restrict__ dst, int B, int k, double scale) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)B * k;
+    if (t >= total) return;
+    const long long b = t / k, p = t % k;
+    dst[t] = ((double)hi[p * B + b] + (double)lo[p * B + b]) * scale;
+}
+
 template <typename R>
 __global__ void convert_kernel(const double* __restrict__ src, R* __restrict__ dst, long long n) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -116,6 +136,21 @@ __global__ void convert_kernel(const double* __restrict__ src, R* __restrict__ d
 }
 
 static inline unsigned blocks_for(long long n) { return (unsigned)((n + 255) / 256); }
+
+cudaError_t launch_split_hi_lo(const double* src, double* dst, int B, int k, cudaStream_t st) {
+    const long long total = (long long)B * k;
+    if (total <= 0) return cudaSuccess;
+    split_hi_lo<<<blocks_for(total), 256, 0, st>>>(src, dst, B, k);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_interleaved_pair(const float* hi, const float* lo, double* dst, int B, int k, double scale,
+                                         cudaStream_t st) {
+    const long long total = (long long)B * k;
+    if (total <= 0) return cudaSuccess;
+    from_interleaved_pair<<<blocks_for(total), 256, 0, st>>>(hi, lo, dst, B, k, scale);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_to_interleaved(const double* src, void* dst, int B, int k, bool f32, cudaStream_t st) {
     const long long total = (long long)B * k;

@@ -28,6 +28,12 @@ cudaError_t launch_gather_cols(const void* src, double* dst, const int* slots, i
 cudaError_t launch_scatter_u32(const unsigned* src, unsigned* dst, const int* slots, int m, cudaStream_t st);
 cudaError_t launch_scatter_i32(const int* src, int* dst, const int* slots, int m, cudaStream_t st);
 cudaError_t launch_scatter_i64(const long long* src, long long* dst, const int* slots, int m, cudaStream_t st);
+// [B][k] double -> [B][2k] double: high parts (v rounded to FP32) then low
+// parts (v minus its high part), the extended-state mode's value split.
+cudaError_t launch_split_hi_lo(const double* src, double* dst, int B, int k, cudaStream_t st);
+// [k][B] FP32 high and low parts -> [B][k] double hi + lo (scaled).
+cudaError_t launch_from_interleaved_pair(const float* hi, const float* lo, double* dst, int B, int k, double scale,
+                                         cudaStream_t st);
 // element-wise double -> compute precision
 cudaError_t launch_convert(const double* src, void* dst, long long n, bool f32, cudaStream_t st);
 

@@ -36,19 +36,84 @@ struct Emitter {
     const Literals& lit;
     std::vector<int> slot;   // parameter -> loaded register slot (-1: literal)
     int nload = 0;
+    // extended-state mode: low parts of the values (loaded into q[], or
+    // literals; a literal 0 drops the term from the low-part functions)
+    bool ext = false;
+    std::vector<int> slot_lo;
+    int nload_lo = 0;
 
-    Emitter(const Pattern& p, const Literals& l) : pat(p), lit(l) {
+    Emitter(const Pattern& p, const Literals& l, bool ext_ = false) : pat(p), lit(l), ext(ext_) {
         const int P = pat.P();
         slot.assign(P, -1);
+        slot_lo.assign(P, -1);
         for (int q = 0; q < P; ++q) {
             bool is_lit = q < (int)lit.is_lit.size() && lit.is_lit[q] && std::isfinite(lit.value[q]);
             if (!is_lit) slot[q] = nload++;
+            if (ext && !lo_is_lit(l, q)) slot_lo[q] = nload_lo++;
         }
+    }
+
+    static bool lo_is_lit(const Literals& l, int q) {
+        return q < (int)l.is_lit_lo.size() && l.is_lit_lo[q] && std::isfinite(l.value_lo[q]);
     }
 
     std::string val(int q) const {
         if (slot[q] >= 0) return "p[" + std::to_string(slot[q]) + "]";
         return hexlit(lit.value[q]);
+    }
+
+    // low part of value q ("" when it is the literal 0)
+    std::string val_lo(int q) const {
+        if (slot_lo[q] >= 0) return "q[" + std::to_string(slot_lo[q]) + "]";
+        if (lit.value_lo[q] == 0.0) return "";
+        return hexlit(lit.value_lo[q]);
+    }
+
+    // rhs_lo body: f = the right-hand side of the low parts of the values, one
+    // fma chain per destination over the terms in canonical order (terms whose
+    // low part is 0 contribute nothing and are left out).
+    void rhs_lo(std::ostringstream& o) const {
+        const int n = pat.n;
+        const int go = pat.k_nnz(), lo = go + pat.g_nnz(), po = lo + pat.l_nnz(), fo = po + pat.p_nnz();
+        std::vector<std::vector<std::pair<std::string, std::string>>> terms(n);
+        auto S = [](int v) { return std::to_string(v); };
+        for (int i = 0; i < n; ++i)
+            for (int q = pat.k_ptr[i]; q < pat.k_ptr[i + 1]; ++q)
+                if (!val_lo(q).empty()) terms[i].push_back({val_lo(q), "xs[" + S(pat.k_col[q]) + "]"});
+        for (int e = 0; e < pat.g_nnz(); ++e) {
+            const int* ix = &pat.g_idx[3 * e];
+            if (val_lo(go + e).empty()) continue;
+            terms[ix[0]].push_back({"m::mul(" + val_lo(go + e) + ", xs[" + S(ix[1]) + "])", "xp[" + S(ix[2]) + "]"});
+        }
+        for (int e = 0; e < pat.l_nnz(); ++e) {
+            const int* ix = &pat.l_idx[4 * e];
+            if (val_lo(lo + e).empty()) continue;
+            terms[ix[0]].push_back({"m::mul(m::mul(" + val_lo(lo + e) + ", xs[" + S(ix[1]) + "]), xp[" + S(ix[2]) +
+                                        "])",
+                                    "xp[" + S(ix[3]) + "]"});
+        }
+        for (int e = 0; e < pat.p_nnz(); ++e) {
+            const int* ix = &pat.p_idx[5 * e];
+            if (val_lo(po + e).empty()) continue;
+            terms[ix[0]].push_back({"m::mul(m::mul(m::mul(" + val_lo(po + e) + ", xs[" + S(ix[1]) + "]), xp[" +
+                                        S(ix[2]) + "]), xp[" + S(ix[3]) + "])",
+                                    "xp[" + S(ix[4]) + "]"});
+        }
+        for (int e = 0; e < pat.f_nnz(); ++e)
+            if (!val_lo(fo + e).empty()) terms[pat.f_idx[e]].push_back({val_lo(fo + e), "u"});
+        for (int i = 0; i < n; ++i) {
+            if (terms[i].empty()) {
+                o << "    f[" << i << "] = R(0);\n";
+                continue;
+            }
+            for (size_t k = 0; k < terms[i].size(); ++k) {
+                if (k == 0)
+                    o << "    f[" << i << "] = m::mul(" << terms[i][k].first << ", " << terms[i][k].second << ");\n";
+                else
+                    o << "    f[" << i << "] = m::fma(" << terms[i][k].first << ", " << terms[i][k].second << ", f["
+                      << i << "]);\n";
+            }
+        }
     }
 
     // rhs body.  Per destination, the terms [K row | Gamma | Lambda | Psi |
@@ -325,7 +390,8 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
     if (const char* e = std::getenv("PASIF_WS_ROLL")) roll = std::atoi(e) != 0;   // tuning override
     std::ostringstream o;
     o << "// generated by pasif_gb300 jit.cpp: warp-sliced "
-      << (mode == 0 ? "forward" : mode == 1 ? "serving pool" : "exact adjoint") << " RK4, n=" << n
+      << (mode == 0 ? "forward" : mode == 1 ? "serving pool" : "exact adjoint") << (key.ext ? " extended state" : "")
+      << " RK4, n=" << n
       << " P=" << pat.P() << " slices=" << sl.L << " published=" << sl.NP << " rolled=" << (roll ? 1 : 0) << "\n";
     o << "#include \"rk4_core.cuh\"\nnamespace pk {\n";
     o << "typedef " << (key.f32 ? "float" : "double") << " R;\n";
@@ -342,11 +408,24 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
                 slot[q] = k;
             }
         };
+        // extended-state mode: low parts of the same values (literal 0: the term drops out)
+        std::map<int, int> slot_lo;
+        auto need_lo = [&](int q) {
+            if (!key.ext || Emitter::lo_is_lit(lit, q) || slot_lo.count(q)) return;
+            const int k = (int)slot_lo.size();
+            slot_lo[q] = k;
+        };
+        auto val_lo = [&](int q) -> std::string {
+            if (slot_lo.count(q)) return "q[" + S(slot_lo[q]) + "]";
+            if (lit.value_lo[q] == 0.0) return "";
+            return hexlit(lit.value_lo[q]);
+        };
         bool forced = false;
         std::vector<int> foreign, pown;   // pown: values of own destinations' terms (gradients kept here)
         for (int i : own)
             for (const Term& t : dt[i]) {
                 need_val(t.q);
+                need_lo(t.q);
                 pown.push_back(t.q);
                 if (t.kind == 4) forced = true;
                 for (int k = 0; k < (t.kind < 4 ? t.kind + 1 : 0); ++k)
@@ -361,6 +440,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
                 for (int k = 0; k < no; ++k) touches = touches || mine(t.ops[k]);
                 if (!touches) continue;
                 need_val(t.q);
+                need_lo(t.q);
                 if (!mine(it.first)) wforeign.push_back(it.first);
                 for (int k = 0; k < no; ++k)
                     if (!mine(t.ops[k])) yforeign.push_back(t.ops[k]);
@@ -381,8 +461,11 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
           << ", SQOWN = " << (w == sl.sq_owner ? "true" : "false") << ", ROLL = " << (roll ? "true" : "false")
           << ";\n";
         o << "  R p[" << std::max<size_t>(slot.size(), 1) << "];\n";
+        if (key.ext) o << "  R q[" << std::max<size_t>(slot_lo.size(), 1) << "];   // low parts of the values\n";
         o << "  __device__ __forceinline__ void load(const R* __restrict__ vals, long long B, int b) {\n";
         for (auto& kv : slot) o << "    p[" << kv.second << "] = vals[" << kv.first << "LL * B + b];\n";
+        for (auto& kv : slot_lo)
+            o << "    q[" << kv.second << "] = vals[" << (pat.P() + kv.first) << "LL * B + b];\n";
         o << "  }\n";
         o << "  template <class V> __device__ __forceinline__ void load_vec(V& X, const R* __restrict__ src, long long B,"
              " int b) const {\n";
@@ -459,6 +542,41 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             o << "    f[" << k << "] = " << (ts.size() >= 2 ? "m::add(a, c)" : "a") << ";\n";
         }
         o << "  }\n";
+        if (key.ext) {   // right-hand side of the low parts: one fma chain per destination
+            o << "  template <class V, class F> __device__ __forceinline__ void rhs_lo(const V& X, const R* buf, R u,"
+                 " F& f) const {\n";
+            o << "    typedef M<R> m;\n";
+            std::vector<int> used;
+            for (int i : own)
+                for (const Term& t : dt[i])
+                    if (!val_lo(t.q).empty())
+                        for (int k = 0; k < (t.kind < 4 ? t.kind + 1 : 0); ++k)
+                            if (!mine(t.ops[k])) used.push_back(t.ops[k]);
+            std::sort(used.begin(), used.end());
+            used.erase(std::unique(used.begin(), used.end()), used.end());
+            for (int j : used) o << "    const R x" << j << " = buf[" << sl.pub[j] * 32 << "];\n";
+            for (int k = 0; k < MM; ++k) {
+                int cnt = 0;
+                for (const Term& t : dt[own[k]]) {
+                    const std::string v = val_lo(t.q);
+                    if (v.empty()) continue;
+                    std::string first, last;
+                    if (t.kind == 4) {
+                        first = v;
+                        last = "u";
+                    } else {
+                        first = v;
+                        for (int z = 0; z < t.kind; ++z) first = "m::mul(" + first + ", " + x(t.ops[z]) + ")";
+                        last = x(t.ops[t.kind]);
+                    }
+                    if (cnt == 0) o << "    f[" << k << "] = m::mul(" << first << ", " << last << ");\n";
+                    else o << "    f[" << k << "] = m::fma(" << first << ", " << last << ", f[" << k << "]);\n";
+                    ++cnt;
+                }
+                if (cnt == 0) o << "    f[" << k << "] = R(0);\n";
+            }
+            o << "    (void)u;\n  }\n";
+        }
         if (adj) {
             auto W = [&](int i) { return mine(i) ? "W[" + S(sl.local[i]) + "]" : "w" + S(i); };
             auto Y = [&](int j) { return mine(j) ? "Y[" + S(sl.local[j]) + "]" : "y" + S(j); };
@@ -507,11 +625,48 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
                 }
             }
             o << "  }\n";
-            o << "  template <bool KAHAN, class V> __device__ __forceinline__ void add_sq_grad(V& LAM, V& CL, const V& QN,"
-                 " R g) const {\n";
+            if (key.ext) {   // J_lo^T W in the scatter order of vjp, no parameter gradients
+                o << "  template <class V> __device__ __forceinline__ void vjp_lo(const V& Y, const R* yb, const V& W,"
+                     " const R* wb, R u, V& out) const {\n";
+                o << "    typedef M<R> m;\n";
+                for (int j : yforeign) o << "    const R y" << j << " = yb[" << sl.pub[j] * 32 << "];\n";
+                for (int i : wforeign) o << "    const R w" << i << " = wb[" << sl.pub[i] * 32 << "];\n";
+                for (int k = 0; k < MM; ++k) o << "    out[" << k << "] = R(0);\n";
+                for (const auto& it : scatter) {
+                    const int i = it.first;
+                    const Term& t = it.second;
+                    const int no = t.kind < 4 ? t.kind + 1 : 0;
+                    const std::string v = val_lo(t.q);
+                    if (v.empty() || t.kind == 4) continue;
+                    if (t.kind == 0) {
+                        const int j = t.ops[0];
+                        if (mine(j)) o << "    " << out(j) << " = m::fma(" << v << ", " << W(i) << ", " << out(j) << ");\n";
+                        continue;
+                    }
+                    bool any = false;
+                    for (int k = 0; k < no; ++k) any = any || mine(t.ops[k]);
+                    if (!any) continue;
+                    o << "    { const R a_ = m::mul(" << v << ", " << W(i) << ");\n";
+                    for (int k = 0; k < no; ++k) {
+                        const int j = t.ops[k];
+                        if (!mine(j)) continue;
+                        std::vector<int> oth;
+                        for (int z = 0; z < no; ++z)
+                            if (z != k) oth.push_back(t.ops[z]);
+                        std::string f = "a_";
+                        for (size_t z = 0; z + 1 < oth.size(); ++z) f = "m::mul(" + f + ", " + Y(oth[z]) + ")";
+                        o << "      " << out(j) << " = m::fma(" << f << ", " << Y(oth.back()) << ", " << out(j) << ");\n";
+                    }
+                    o << "    }\n";
+                }
+                o << "    (void)u;\n  }\n";
+            }
+            o << "  template <bool KAHAN, bool EXT, class V> __device__ __forceinline__ void add_sq_grad(V& LAM, V& CL,"
+                 " const V& QN, R g) const {\n";
             for (int k = 0; k < MM; ++k)
                 if (own[k] < 64 && ((key.sq_mask >> own[k]) & 1ull))
-                    o << "    if (KAHAN) kahan_add(LAM[" << k << "], CL[" << k << "], M<R>::mul(g, QN[" << k
+                    o << "    if (EXT) ext_add(LAM[" << k << "], CL[" << k << "], M<R>::mul(g, QN[" << k
+                      << "])); else if (KAHAN) kahan_add(LAM[" << k << "], CL[" << k << "], M<R>::mul(g, QN[" << k
                       << "])); else LAM[" << k << "] = M<R>::fma(g, QN[" << k << "], LAM[" << k << "]);\n";
             o << "  }\n";
             o << "  template <class PV> __device__ __forceinline__ void store_pbar(const PV& PB, double* pbar, long long B,"
@@ -525,16 +680,18 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             o << "  __device__ __forceinline__ void zero_pbar(double* pbar, long long B, int b) const {\n";
             for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = 0.0;\n";
             o << "  }\n";
-            o << "  template <class PV> __device__ __forceinline__ void add_pbar(const PV& ps, double* pbar, long long B,"
-                 " int b) const {\n";
+            o << "  template <bool SC, class PV> __device__ __forceinline__ void add_pbar(const PV& ps, double* pbar,"
+                 " long long B, int b, double s) const {\n";
             for (auto& kv : pslot)
-                o << "    pbar[" << kv.first << "LL * B + b] = pbar[" << kv.first << "LL * B + b] + (double)ps["
+                o << "    pbar[" << kv.first << "LL * B + b] = SC ? M<double>::fma(s, (double)ps[" << kv.second
+                  << "], pbar[" << kv.first << "LL * B + b]) : pbar[" << kv.first << "LL * B + b] + (double)ps["
                   << kv.second << "];\n";
             o << "  }\n";
         }
         o << "};\n";
     }
     o << "}  // namespace pk\n";
+    const std::string ext = key.ext ? "true" : "false";
     const std::string kahan = key.kahan ? "true" : "false", hmax = key.max_mask ? "true" : "false",
                       hsq = key.sq_mask ? "true" : "false", htraj = std::to_string(key.traj);
     const char* sig = mode == 0 ? "pk_fwd(pk::FwdArgs<pk::R> a)" : mode == 1 ? "pk_pool(pk::PoolArgs<pk::R> p)"
@@ -553,11 +710,11 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
         if (mode == 1)
             o << "ws_pool<R, " << kahan << ", " << hmax << ", " << hsq << ", " << n << ">(sl, p, sm, b, valid, w);";
         else if (mode == 0)
-            o << "ws_fwd<R, " << kahan << ", " << hmax << ", " << hsq << ", " << htraj << ", " << n
+            o << "ws_fwd<R, " << kahan << ", " << hmax << ", " << hsq << ", " << htraj << ", " << n << ", " << ext
               << ">(sl, a, sm, b, valid);";
         else   // the Kahan mode of the forward passes is the plan's (AdjArgs::kahan)
-            o << "ws_adj<R, " << kahan << ", " << hsq << ", " << (key.f32 ? "true" : "false") << ", " << n
-              << ">(sl, a, sm, b, valid);";
+            o << "ws_adj<R, " << kahan << ", " << hsq << ", " << (key.f32 ? "true" : "false") << ", " << n << ", "
+              << ext << ">(sl, a, sm, b, valid);";
         o << " } break;\n";
     }
     o << "    default: break;\n  }\n}\n";
@@ -595,31 +752,19 @@ static void emit_sample_ring(std::ostringstream& o, int W, int block, const Patt
         o << "  __device__ static R* ring() { return nullptr; }\n";
 }
 
+namespace {
+void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32);
+}
+
 std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key) {
     if (key.slices >= 2) return ws_source(pat, lit, key, 0);
-    Emitter em(pat, lit);
+    Emitter em(pat, lit, key.ext);
     const int n = pat.n;
     std::ostringstream o;
-    o << "// generated by pasif_gb300 jit.cpp: forward RK4, n=" << n << " P=" << pat.P() << "\n";
-    o << "#include \"rk4_core.cuh\"\n";
-    o << "namespace pk {\n";
-    o << "typedef " << (key.f32 ? "float" : "double") << " R;\n";
-    o << "struct JSys {\n";
-    o << "  R p[" << (em.nload > 0 ? em.nload : 1) << "];\n";
-    o << "  __device__ static constexpr int dim() { return " << n << "; }\n";
-    o << "  __device__ __forceinline__ void load(const R* __restrict__ vals, long long B, int b) {\n";
-    for (int q = 0; q < pat.P(); ++q)
-        if (em.slot[q] >= 0) o << "    p[" << em.slot[q] << "] = vals[" << q << "LL * B + b];\n";
-    o << "  }\n";
-    o << "  template <bool FORCE, class V, class W, class F>\n";
-    o << "  __device__ __forceinline__ void rhs(const V& xs, const W& xp, R u, F& f) const {\n";
-    o << "    typedef M<R> m;\n    R a, c;\n";
-    o << "    if (FORCE) {\n";
-    em.rhs(o, true);
-    o << "    } else {\n";
-    em.rhs(o, false);
-    o << "    }\n";
-    o << "  }\n};\n";
+    o << "// generated by pasif_gb300 jit.cpp: forward RK4, n=" << n << " P=" << pat.P()
+      << (key.ext ? " extended state" : "") << "\n";
+    emit_sys_head(o, pat, em, key.f32);
+    o << "};\n";
     // forcing window and weights as compile-time constants
     const int W = key.window;
     o << "struct JW {\n  static constexpr int W = " << W << ";\n";
@@ -639,7 +784,7 @@ std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelK
     o << "  RegVec<R, " << n << "> Q, Cm, S, K, Mi, Mx;\n";
     o << "  fwd_run_iv<R, " << n << ", " << (key.kahan ? "true" : "false") << ", "
       << (key.max_mask ? "true" : "false") << ", " << (key.sq_mask ? "true" : "false") << ", "
-      << key.traj << ", JW>(sys, a, b, "
+      << key.traj << ", JW, " << (key.ext ? "true" : "false") << ">(sys, a, b, "
       << key.max_mask << "ull, " << key.sq_mask << "ull, Q, Cm, S, K, Mi, Mx);\n";
     o << "}\n";
     return o.str();
@@ -660,11 +805,22 @@ void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em,
     o << "typedef " << (f32 ? "float" : "double") << " R;\n";
     o << "struct JSys {\n";
     o << "  R p[" << (em.nload > 0 ? em.nload : 1) << "];\n";
+    if (em.ext) o << "  R q[" << (em.nload_lo > 0 ? em.nload_lo : 1) << "];   // low parts of the values\n";
     o << "  __device__ static constexpr int dim() { return " << pat.n << "; }\n";
     o << "  __device__ __forceinline__ void load(const R* __restrict__ vals, long long B, int b) {\n";
     for (int q = 0; q < pat.P(); ++q)
         if (em.slot[q] >= 0) o << "    p[" << em.slot[q] << "] = vals[" << q << "LL * B + b];\n";
+    for (int q = 0; q < pat.P(); ++q)
+        if (em.ext && em.slot_lo[q] >= 0)
+            o << "    q[" << em.slot_lo[q] << "] = vals[" << (pat.P() + q) << "LL * B + b];\n";
     o << "  }\n";
+    if (em.ext) {
+        o << "  template <bool FORCE, class V, class W, class F>\n";
+        o << "  __device__ __forceinline__ void rhs_lo(const V& xs, const W& xp, R u, F& f) const {\n";
+        o << "    typedef M<R> m;\n";
+        em.rhs_lo(o);
+        o << "  }\n";
+    }
     o << "  template <bool FORCE, class V, class W, class F>\n";
     o << "  __device__ __forceinline__ void rhs(const V& xs, const W& xp, R u, F& f) const {\n";
     o << "    typedef M<R> m;\n    R a, c;\n";
@@ -729,6 +885,57 @@ void emit_vjp(std::ostringstream& o, const Pattern& pat, const Emitter& em) {
     o << "  }\n";
 }
 
+// vjp_lo: out = J_lo(y)^T w, the transposed Jacobian of the low parts of the
+// values, in the scatter order of emit_vjp (no parameter gradients; terms
+// whose low part is 0 are left out).
+void emit_vjp_lo(std::ostringstream& o, const Pattern& pat, const Emitter& em) {
+    const int n = pat.n;
+    const int go = pat.k_nnz(), lo = go + pat.g_nnz(), po = lo + pat.l_nnz();
+    auto s = [](int v) { return std::to_string(v); };
+    o << "  template <class V, class W, class O>\n";
+    o << "  __device__ __forceinline__ void vjp_lo(const V& y, const W& w, R u, O& out) const {\n";
+    o << "    typedef M<R> m;\n";
+    for (int i = 0; i < n; ++i) o << "    out[" << i << "] = R(0);\n";
+    for (int i = 0; i < n; ++i)
+        for (int q = pat.k_ptr[i]; q < pat.k_ptr[i + 1]; ++q) {
+            if (em.val_lo(q).empty()) continue;
+            const std::string j = s(pat.k_col[q]);
+            o << "    out[" << j << "] = m::fma(" << em.val_lo(q) << ", w[" << i << "], out[" << j << "]);\n";
+        }
+    for (int e = 0; e < pat.g_nnz(); ++e) {
+        if (em.val_lo(go + e).empty()) continue;
+        const int* ix = &pat.g_idx[3 * e];
+        const std::string i = s(ix[0]), j = s(ix[1]), k = s(ix[2]);
+        o << "    { const R a_ = m::mul(" << em.val_lo(go + e) << ", w[" << i << "]);\n";
+        o << "      out[" << j << "] = m::fma(a_, y[" << k << "], out[" << j << "]);\n";
+        o << "      out[" << k << "] = m::fma(a_, y[" << j << "], out[" << k << "]); }\n";
+    }
+    for (int e = 0; e < pat.l_nnz(); ++e) {
+        if (em.val_lo(lo + e).empty()) continue;
+        const int* ix = &pat.l_idx[4 * e];
+        const std::string i = s(ix[0]), j = s(ix[1]), k = s(ix[2]), l = s(ix[3]);
+        o << "    { const R a_ = m::mul(" << em.val_lo(lo + e) << ", w[" << i << "]);\n";
+        o << "      out[" << j << "] = m::fma(m::mul(a_, y[" << k << "]), y[" << l << "], out[" << j << "]);\n";
+        o << "      out[" << k << "] = m::fma(m::mul(a_, y[" << j << "]), y[" << l << "], out[" << k << "]);\n";
+        o << "      out[" << l << "] = m::fma(m::mul(a_, y[" << j << "]), y[" << k << "], out[" << l << "]); }\n";
+    }
+    for (int e = 0; e < pat.p_nnz(); ++e) {
+        if (em.val_lo(po + e).empty()) continue;
+        const int* ix = &pat.p_idx[5 * e];
+        const std::string i = s(ix[0]), j = s(ix[1]), k = s(ix[2]), l = s(ix[3]), mm = s(ix[4]);
+        o << "    { const R a_ = m::mul(" << em.val_lo(po + e) << ", w[" << i << "]);\n";
+        o << "      out[" << j << "] = m::fma(m::mul(m::mul(a_, y[" << k << "]), y[" << l << "]), y[" << mm << "], out["
+          << j << "]);\n";
+        o << "      out[" << k << "] = m::fma(m::mul(m::mul(a_, y[" << j << "]), y[" << l << "]), y[" << mm << "], out["
+          << k << "]);\n";
+        o << "      out[" << l << "] = m::fma(m::mul(m::mul(a_, y[" << j << "]), y[" << k << "]), y[" << mm << "], out["
+          << l << "]);\n";
+        o << "      out[" << mm << "] = m::fma(m::mul(m::mul(a_, y[" << j << "]), y[" << k << "]), y[" << l << "], out["
+          << mm << "]); }\n";
+    }
+    o << "    (void)u;\n  }\n";
+}
+
 // The cache lock is not held while NVRTC compiles (up to a second for a large
 // pattern): the host threads of a server keep launching cached kernels while
 // another thread compiles a new one.  Two threads compiling the same source
@@ -788,20 +995,23 @@ bool compile_report(const std::string& src, std::string* report, std::string* er
 }
 
 std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, int slices,
-                       bool kahan) {
+                       bool kahan, bool ext) {
     if (slices >= 2) {
         FwdKernelKey key;
         key.f32 = f32;
         key.kahan = kahan;
         key.sq_mask = sq_mask;
         key.slices = slices;
+        key.ext = ext;
         return ws_source(pat, lit, key, 2);
     }
-    Emitter em(pat, lit);
+    Emitter em(pat, lit, ext);
     std::ostringstream o;
-    o << "// generated by pasif_gb300 jit.cpp: exact adjoint, n=" << pat.n << " P=" << pat.P() << "\n";
+    o << "// generated by pasif_gb300 jit.cpp: exact adjoint, n=" << pat.n << " P=" << pat.P()
+      << (ext ? " extended state" : "") << "\n";
     emit_sys_head(o, pat, em, f32);
     emit_vjp(o, pat, em);
+    if (ext) emit_vjp_lo(o, pat, em);
     o << "};\n}  // namespace pk\n";
     o << "extern \"C\" __global__ void __launch_bounds__(128) pk_adj(pk::AdjArgs<pk::R> a) {\n";
     o << "  using namespace pk;\n";
@@ -811,8 +1021,8 @@ std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsign
     const int P = pat.P() > 0 ? pat.P() : 1;
     if (f32) {
         o << "  RegVec<R, " << P << "> pacc;\n";
-        o << "  adj_run_jit<R, " << pat.n << ", " << P << ", " << (sq_mask ? "true" : "false") << ", true>(sys, a, b, "
-          << sq_mask << "ull, pacc);\n";
+        o << "  adj_run_jit<R, " << pat.n << ", " << P << ", " << (sq_mask ? "true" : "false") << ", true, "
+          << (ext ? "true" : "false") << ">(sys, a, b, " << sq_mask << "ull, pacc);\n";
     } else {
         o << "  GVec<double> pacc{a.pbar + b, (long long)a.B};\n";
         o << "  adj_run_jit<R, " << pat.n << ", " << P << ", " << (sq_mask ? "true" : "false")
@@ -862,12 +1072,12 @@ bool get_pool_kernel(const Pattern& pat, const FwdKernelKey& key, JitKernel* out
 }
 
 bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, bool kahan, unsigned long long sq_mask, int slices,
-                    JitKernel* out, std::string* err) {
+                    JitKernel* out, std::string* err, bool ext) {
     if (pat.n <= 0 || pat.n > (slices >= 2 ? kWsMaxN : kJitMaxN) || pat.P() > (slices >= 2 ? 8192 : 1024)) {
         *err = "pattern outside the specialised range";
         return false;
     }
-    return get_cached(adj_source(pat, lit, f32, sq_mask, slices, kahan), "pk_adj", 128, out, err);
+    return get_cached(adj_source(pat, lit, f32, sq_mask, slices, kahan, ext), "pk_adj", 128, out, err);
 }
 
 bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, JitKernel* out,
@@ -879,7 +1089,7 @@ bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey&
     return get_cached(fwd_source(pat, lit, key), "pk_fwd", key.block, out, err);
 }
 
-int ws_slices(const Pattern& pat, bool f32, bool force, int B) {
+int ws_slices(const Pattern& pat, bool f32, bool force, int B, bool ext) {
     const int n = pat.n;
     // Measured crossovers on GB300 (time sliced / thread per system, 4096 systems):
     // FP32 forward sliced from 28 states (16-state chain 1.34, 28 states 0.94).
@@ -891,20 +1101,20 @@ int ws_slices(const Pattern& pat, bool f32, bool force, int B) {
         const bool small_batch = B > 0 && B <= 8192;
         if (f32 ? n < 28 : (n < 3 || (n < 8 && !small_batch))) return 0;
     }
-    return ws_split(n, f32, force, false);
+    return ws_split(n, f32, force, false, ext);
 }
 
-int ws_slices_adjoint(const Pattern& pat, bool f32, bool force) {
+int ws_slices_adjoint(const Pattern& pat, bool f32, bool force, bool ext) {
     const int n = pat.n;
     // The adjoint keeps about twice the vectors of the forward.  Measured on
     // GB300 (time sliced / thread per system, 1024-4096 systems): FP32 5
     // states 0.75, 8 states 0.62, 4 states 0.93, 2 states 1.12; FP64 2 states
     // 0.68, 4-8 states 0.33-0.44.
     if (n < 2 || n > kWsMaxN || (!force && f32 && n < 5)) return 0;
-    return ws_split(n, f32, force, true);
+    return ws_split(n, f32, force, true, ext);
 }
 
-int ws_split(int n, bool f32, bool force, bool adjoint) {
+int ws_split(int n, bool f32, bool force, bool adjoint, bool ext) {
     // Forward: four warps when the registers allow (up to 32 FP32 / 16 FP64
     // components per warp): each SM sub-partition then runs one slice's code.
     // Measured on GB300 (forward, FP32-Kahan): 128-state chain 4 warps 1.86e9
@@ -916,7 +1126,10 @@ int ws_split(int n, bool f32, bool force, bool adjoint) {
     // system-steps/s): 64-state banded 6 warps 208, 8 warps 176, 12 warps 119;
     // 32-state chain 4 warps 770, 6 warps 740; 128-state chain 8 warps 134, 12
     // warps 89.  (512 systems, 16 blocks, prefer more warps by 5-10 %.)
-    const int cpw = force ? 2 : adjoint ? (f32 ? 11 : 6) : (f32 ? 32 : 16);   // components per warp
+    // the extended-state mode holds the low parts of the values and the
+    // state besides: fewer components per warp (ptxas, 64-state banded system:
+    // 4 warps spill 428 bytes forward, 3.9 KB adjoint)
+    const int cpw = force ? 2 : adjoint ? (f32 ? (ext ? 8 : 11) : 6) : (f32 ? (ext ? 12 : 32) : 16);
     int L = std::max(4, (n + cpw - 1) / cpw);
     if (adjoint && f32 && !force) L = std::min(L, 8);
     if (const char* e = std::getenv("PASIF_WS_SLICES")) L = std::atoi(e);   // tuning override

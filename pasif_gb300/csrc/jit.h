@@ -15,6 +15,11 @@ namespace pasif {
 struct Literals {
     std::vector<unsigned char> is_lit;   // size P
     std::vector<double> value;           // size P (meaningful where is_lit)
+    // Extended-state mode: the same for the low parts of the FP64 values
+    // (v - (float)v, rounded to FP32); a term whose low part is the literal 0
+    // drops out of the low-part right-hand side.
+    std::vector<unsigned char> is_lit_lo;
+    std::vector<double> value_lo;
 };
 
 struct FwdKernelKey {
@@ -27,6 +32,7 @@ struct FwdKernelKey {
     int window = 0;                 // forcing window (0 = sample and hold)
     std::vector<double> wn, wc;     // its weights in the compute precision
     int slices = 0;                 // >= 2: warp-sliced kernel with that many warps per 32 systems
+    bool ext = false;               // extended-state mode (FP32 stages, double-float state, low parts of the values)
 };
 
 struct JitKernel {
@@ -41,11 +47,11 @@ struct JitKernel {
 // Warps per 32 systems of the warp-sliced kernels for a pattern: 0 (thread
 // per system) where that layout is faster (small systems in FP32), unless
 // `force`.  B: systems per launch (0: unknown, taken as large).
-int ws_slices(const Pattern& pat, bool f32, bool force, int B = 0);
+int ws_slices(const Pattern& pat, bool f32, bool force, int B = 0, bool ext = false);
 // Same for the exact adjoint (sliced from smaller systems).
-int ws_slices_adjoint(const Pattern& pat, bool f32, bool force);
+int ws_slices_adjoint(const Pattern& pat, bool f32, bool force, bool ext = false);
 // Warps for n components (2..16).
-int ws_split(int n, bool f32, bool force, bool adjoint);
+int ws_split(int n, bool f32, bool force, bool adjoint, bool ext = false);
 
 // Source of the forward kernel for a pattern (exposed for tests and docs).
 std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key);
@@ -58,10 +64,9 @@ bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey&
 // Source and cached kernel of the exact adjoint (AdjArgs) for a pattern.
 // (slices >= 2: warp-sliced, with the forward passes' Kahan mode compiled in)
 std::string adj_source(const Pattern& pat, const Literals& lit, bool f32, unsigned long long sq_mask, int slices = 0,
-                       bool kahan = false);
+                       bool kahan = false, bool ext = false);
 bool get_adj_kernel(const Pattern& pat, const Literals& lit, bool f32, bool kahan, unsigned long long sq_mask, int slices,
-                    JitKernel* out,
-                    std::string* err);
+                    JitKernel* out, std::string* err, bool ext = false);
 // Serving-pool chunk kernel (PoolArgs): values always loaded, no literals.
 std::string pool_source(const Pattern& pat, const FwdKernelKey& key);
 bool get_pool_kernel(const Pattern& pat, const FwdKernelKey& key, JitKernel* out, std::string* err);

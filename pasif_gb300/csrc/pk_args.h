@@ -58,6 +58,12 @@ struct FwdArgs {
     // kernels store the state and compensation before every step t with
     // t % traj_every == 0 to traj + (t / traj_every) [2n][B].
     const R* comp;
+    // Extended-state mode (FP32 stages, double-float state): comp holds the
+    // initial low parts, comp_out receives the final ones ([n][B]), vals holds
+    // [2P][B] (high parts, then the low parts of the FP64 values), and h6lo is
+    // the low part of h/6 (h/6 = h6 + h6lo to about 48 bits).
+    R* comp_out;
+    R h6lo;
 };
 
 // Serving pool: C slots of one pattern, each slot an instance of some request
@@ -116,7 +122,7 @@ struct AdjArgs {
     int phase;
     int t_begin, t_end;
     int k_lo, k_hi;
-    R* lamc;                    // [n][B] (Kahan mode)
+    R* lamc;                    // [n][B] (Kahan mode; extended-state mode: low parts of the adjoint state)
     // Stored trajectory: buf already holds the slots of steps slot_base ..
     // (slot t - slot_base) and the state after the last of them (state part of
     // the next slot), written by a forward kernel launched first, so there is
@@ -124,6 +130,11 @@ struct AdjArgs {
     // group the backward launches.  slot_base = 0: the whole trajectory.
     int stored;
     int slot_base;
+    // Extended-state mode: vals [2P][B] (high, low parts), x0 [2n][B] (high,
+    // low parts), h6lo the low part of h/6; parameter gradients are summed
+    // per step without the h/6 factor and added as (h6 + h6lo) * sum in FP64.
+    int ext;
+    R h6lo;
 };
 
 // __GpuDriver::_getGradient semantics (see the oracle for the quirk list).

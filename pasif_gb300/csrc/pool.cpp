@@ -49,6 +49,7 @@ int Pool::create(const Pattern& pat, int precision, int window, const double* im
         return 1;
     }
     if (!(h > 0.0)) { *err = "time step must be positive"; return 1; }
+    if (precision == kFP32Ext) { *err = "serving pools run FP64, FP32 or FP32 with compensated update"; return 1; }
     std::unique_ptr<Pool> p(new Pool());
     int rc = plan_create(pat, precision, false, &p->plan_, err);
     if (rc) return rc;

@@ -121,6 +121,40 @@ __device__ __forceinline__ void kahan_add(R& s, R& c, R inc) {
     s = t;
 }
 
+// Extended-state mode: the state is an unevaluated FP32 pair hi + lo (about
+// 48 significant bits).  (hi, lo) += h6 sum + h cr with h/6 = h6 + h6lo: the
+// rounding error of the product h6 sum (an fma), the low part of h/6 and the
+// FP64-residual term h cr are collected in e; hi + p is split exactly
+// (two-sum) and the low parts are renormalised into lo (fast two-sum).
+template <typename R>
+__device__ __forceinline__ void ext_update(R& hi, R& lo, R sum, R cr, R h, R h6, R h6lo) {
+    typedef M<R> m;
+    const R p = m::mul(h6, sum);
+    R e = m::fma(h6, sum, -p);
+    e = m::fma(h6lo, sum, e);
+    e = m::fma(h, cr, e);
+    const R t = m::add(hi, p);
+    const R z = m::sub(t, hi);
+    const R err = m::add(m::sub(hi, m::sub(t, z)), m::sub(p, z));
+    const R l = m::add(lo, m::add(err, e));
+    const R q = m::add(t, l);
+    lo = m::sub(l, m::sub(q, t));
+    hi = q;
+}
+
+// (hi, lo) += x (two-sum, renormalised).
+template <typename R>
+__device__ __forceinline__ void ext_add(R& hi, R& lo, R x) {
+    typedef M<R> m;
+    const R t = m::add(hi, x);
+    const R z = m::sub(t, hi);
+    const R err = m::add(m::sub(hi, m::sub(t, z)), m::sub(x, z));
+    const R l = m::add(lo, err);
+    const R q = m::add(t, l);
+    lo = m::sub(l, m::sub(q, t));
+    hi = q;
+}
+
 __device__ __forceinline__ void pacc_add(double& p, double x, double y) { p = __fma_rn(x, y, p); }
 __device__ __forceinline__ void pacc_add(double& p, float x, float y) { p = __fma_rn((double)x, (double)y, p); }
 __device__ __forceinline__ void pacc_add(float& p, float x, float y) { p = __fmaf_rn(x, y, p); }
@@ -258,15 +292,24 @@ struct GenSys {
 // NSTG = 1: the step's state is also stored to stg[i sB]; NSTG = 4: and its
 // stage inputs Y2, Y3, Y4 to stg[(j n + i) sB], j = 1..3: one slot of an
 // adjoint trajectory (adj_slot_vecs).
-template <typename R, int N, bool KAHAN, int NSTG = 0, class Sys, class V>
+// EXT (extended-state mode, N > 0 only): Q and Cm are the high and low parts
+// of the state; the stages use the FP32 values (high parts) of the state and
+// the parameters; the step adds, beside h/6 (k1 + 2k2 + 2k3 + k4), the term
+// h f_lo(Q) of the low parts of the FP64 parameters (JSys::rhs_lo), evaluated
+// once at the start of the step, with ext_update (h6lo: low part of h/6).
+template <typename R, int N, bool KAHAN, int NSTG = 0, bool EXT = false, class Sys, class V>
 __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K, V& Mi,
-                                         R ua, R ub, R uc, R h, R h2, R h6, R* stg = nullptr, long long sB = 0) {
+                                         R ua, R ub, R uc, R h, R h2, R h6, R* stg = nullptr, long long sB = 0,
+                                         R h6lo = R(0)) {
     typedef M<R> m;
+    static_assert(!EXT || N > 0, "extended-state steps need a compile-time state size");
     const int n = N ? N : sys.dim();
     if constexpr (NSTG >= 1) {
 #pragma unroll
         for (int i = 0; i < n; ++i) stg[i * sB] = Q[i];
     }
+    RegVec<R, (EXT && N > 0) ? N : 1> Kc;
+    if constexpr (EXT) sys.template rhs_lo<true>(Q, Q, ua, Kc);
     sys.template rhs<true>(Q, Q, ua, K);
 #pragma unroll
     for (int i = 0; i < n; ++i) { S[i] = K[i]; Mi[i] = m::fma(h2, K[i], Q[i]); }
@@ -292,7 +335,9 @@ __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K
 #pragma unroll
     for (int i = 0; i < n; ++i) {
         const R sum = m::add(S[i], K[i]);
-        if (KAHAN) {
+        if constexpr (EXT) {
+            ext_update(Q[i], Cm[i], sum, Kc[i], h, h6, h6lo);
+        } else if (KAHAN) {
             const R inc = m::mul(h6, sum);
             const R y = m::sub(inc, Cm[i]);
             const R t = m::add(Q[i], y);
@@ -425,7 +470,8 @@ struct RunCtx {
 // a.traj ([step - step0][adj_slot_vecs][N][B], see rk4_step); 3 checkpoints
 // for the adjoint: the state and compensation before every traj_every-th
 // step into a.traj ([step / traj_every][2N][B]).
-template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, class WP, class Sys, class V>
+template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, class WP, bool EXT = false, class Sys,
+          class V>
 __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a, const Forcing<R>& frc, int b,
                                             const RunCtx& rc, unsigned long long max_mask,
                                             unsigned long long sq_mask, V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx,
@@ -487,9 +533,9 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     const unsigned end = rc.step0 + rc.nsteps;
     while (s < end && (s % SPI) != 0u) {
         pre(s);
-        rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
-                                   force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6,
-                                   slot(s), B);
+        rk4_step<R, N, KAHAN, STG, EXT>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
+                                        force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2,
+                                        a.h6, slot(s), B, a.h6lo);
         post(s);
         ++s;
     }
@@ -536,7 +582,8 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
                     else un = g1 ? m::fma(WP::wc(0), x1, m::mul(WP::wn(0), x2)) : R(0);
                 }
                 pre(s + (unsigned)r);
-                rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6, slot(s + (unsigned)r), B);
+                rk4_step<R, N, KAHAN, STG, EXT>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6,
+                                                slot(s + (unsigned)r), B, a.h6lo);
                 post(s + (unsigned)r);
                 uc = un;
             }
@@ -548,9 +595,9 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     }
     while (s < end) {
         pre(s);
-        rk4_step<R, N, KAHAN, STG>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
-                                   force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2, a.h6,
-                                   slot(s), B);
+        rk4_step<R, N, KAHAN, STG, EXT>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
+                                        force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2,
+                                        a.h6, slot(s), B, a.h6lo);
         post(s);
         ++s;
     }
@@ -559,7 +606,8 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
 // One batch instance over the whole horizon (initial state in a.state, final
 // state and reducers out).  HTRAJ as fwd_core_iv; 2 also stores the final
 // state in slot nsteps (its state part).
-template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, class WP, class Sys, class V>
+template <typename R, int N, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, class WP, bool EXT = false, class Sys,
+          class V>
 __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, int b,
                                            unsigned long long max_mask, unsigned long long sq_mask,
                                            V& Q, V& Cm, V& S, V& K, V& Mi, V& Mx) {
@@ -577,10 +625,14 @@ __device__ __forceinline__ void fwd_run_iv(const Sys& sys, const FwdArgs<R>& a, 
     rc.nsteps = (unsigned)a.nsteps;
     rc.max_start = a.max_start;
     rc.sq_start = a.sq_start;
-    fwd_core_iv<R, N, KAHAN, HMAX, HSQ, HTRAJ, WP>(sys, a, a.frc, b, rc, max_mask, sq_mask, Q, Cm, S, K, Mi, Mx, sq,
-                                                   sqc);
+    fwd_core_iv<R, N, KAHAN, HMAX, HSQ, HTRAJ, WP, EXT>(sys, a, a.frc, b, rc, max_mask, sq_mask, Q, Cm, S, K, Mi, Mx,
+                                                        sq, sqc);
 #pragma unroll
     for (int i = 0; i < N; ++i) a.state[i * B + b] = Q[i];
+    if (EXT && a.comp_out) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) a.comp_out[i * B + b] = Cm[i];
+    }
     if (HTRAJ == 2) {
 #pragma unroll
         for (int i = 0; i < N; ++i) a.traj[((long long)a.nsteps * adj_slot_vecs<R>() * N + i) * B + b] = Q[i];
@@ -647,7 +699,7 @@ __device__ __forceinline__ void pool_run_iv(const Sys& sys, const PoolArgs<R>& p
 // PACC = RegVec<float, P> (FP32: parameter gradients summed per step in FP32,
 // then added to the FP64 totals) or GVec<double> (FP64: straight into the
 // FP64 totals, bit-identical to the generic kernel and the oracle).
-template <typename R, int N, int P, bool HSQ, bool STEP_ACC, class Sys, class PACC>
+template <typename R, int N, int P, bool HSQ, bool STEP_ACC, bool EXT = false, class Sys, class PACC>
 __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a, int b, unsigned long long sq_mask,
                                             PACC& pacc) {
     typedef M<R> m;
@@ -665,7 +717,7 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
         if (t0 == 0) {
             for (int p = 0; p < P; ++p) PB[p] = 0.0;
 #pragma unroll
-            for (int i = 0; i < N; ++i) { Q[i] = a.x0[i * B + b]; Cm[i] = R(0); }
+            for (int i = 0; i < N; ++i) { Q[i] = a.x0[i * B + b]; Cm[i] = EXT ? a.x0[(N + i) * B + b] : R(0); }
         } else {
             const R* ck = a.ckpt + (long long)(t0 / a.C) * 2 * N * B + b;
 #pragma unroll
@@ -681,7 +733,8 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
             const R ua = force_at(a.frc, ebase, st, 0u, 0u);
             const R ub = force_at(a.frc, ebase, st, 0u, 1u);
             const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-            if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
+            if constexpr (EXT) rk4_step<R, N, true, 0, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, nullptr, 0, a.h6lo);
+            else if (a.kahan) rk4_step<R, N, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
             else rk4_step<R, N, false>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6);
         }
         if (a.phase == 1) {   // the next segment starts from this checkpoint
@@ -715,6 +768,7 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
         }
     }
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
+    const double h6d = (double)a.h6 + (double)a.h6lo;   // h/6 (extended-state mode)
     for (int k = khi; k >= klo; --k) {
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
@@ -729,7 +783,8 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
                 const R ua = force_at(a.frc, ebase, st, 0u, 0u);
                 const R ub = force_at(a.frc, ebase, st, 0u, 1u);
                 const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-                if (a.kahan) rk4_step<R, N, true, SV>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, bt, B);
+                if constexpr (EXT) rk4_step<R, N, true, SV, true>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, bt, B, a.h6lo);
+                else if (a.kahan) rk4_step<R, N, true, SV>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, bt, B);
                 else rk4_step<R, N, false, SV>(sys, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, bt, B);
             }
         } else {
@@ -789,7 +844,8 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
 #pragma unroll
                 for (int i = 0; i < N; ++i)
                     if (i < 64 && ((sq_mask >> i) & 1ull)) {
-                        if (a.kahan) kahan_add(LAM[i], CL[i], m::mul(gsq2h, QN[i]));
+                        if constexpr (EXT) ext_add(LAM[i], CL[i], m::mul(gsq2h, QN[i]));
+                        else if (a.kahan) kahan_add(LAM[i], CL[i], m::mul(gsq2h, QN[i]));
                         else LAM[i] = m::fma(gsq2h, QN[i], LAM[i]);
                     }
             }
@@ -815,43 +871,55 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
             // from 0 and then added with compensation (Kahan mode)
 #pragma unroll
             for (int i = 0; i < N; ++i) {
-                KB[i] = m::mul(a.h6, LAM[i]);
+                KB[i] = EXT ? LAM[i] : m::mul(a.h6, LAM[i]);
                 QB[i] = a.kahan ? R(0) : LAM[i];
             }
+            // extended-state mode: the stage weights carry no h/6 (it multiplies the
+            // step's sum in ext_update and the parameter sums below), and the
+            // adjoint of the once-per-step term h f_lo(QC) adds h J_lo(QC)^T LAM
+            RegVec<R, EXT ? N : 1> YC;
+            if constexpr (EXT) sys.vjp_lo(QC, LAM, ua, YC);
             sys.vjp(Y4, KB, uc, YB, pacc);
 #pragma unroll
             for (int i = 0; i < N; ++i) {
-                const R sb = m::mul(a.h6, LAM[i]);
+                const R sb = EXT ? LAM[i] : m::mul(a.h6, LAM[i]);
                 QB[i] = m::add(QB[i], YB[i]);
                 KB[i] = m::fma(a.h, YB[i], m::mul(R(2), sb));
             }
             sys.vjp(Y3, KB, ub, YB, pacc);
 #pragma unroll
             for (int i = 0; i < N; ++i) {
-                const R sb = m::mul(a.h6, LAM[i]);
+                const R sb = EXT ? LAM[i] : m::mul(a.h6, LAM[i]);
                 QB[i] = m::add(QB[i], YB[i]);
                 KB[i] = m::fma(a.h2, YB[i], m::mul(R(2), sb));
             }
             sys.vjp(Y2, KB, ub, YB, pacc);
 #pragma unroll
             for (int i = 0; i < N; ++i) {
-                const R sb = m::mul(a.h6, LAM[i]);
+                const R sb = EXT ? LAM[i] : m::mul(a.h6, LAM[i]);
                 QB[i] = m::add(QB[i], YB[i]);
                 KB[i] = m::fma(a.h2, YB[i], sb);
             }
             sys.vjp(QC, KB, ua, YB, pacc);
 #pragma unroll
             for (int i = 0; i < N; ++i) {
-                if (a.kahan) kahan_add(LAM[i], CL[i], m::add(QB[i], YB[i]));
+                if constexpr (EXT) ext_update(LAM[i], CL[i], m::add(QB[i], YB[i]), YC[i], a.h, a.h6, a.h6lo);
+                else if (a.kahan) kahan_add(LAM[i], CL[i], m::add(QB[i], YB[i]));
                 else LAM[i] = m::add(QB[i], YB[i]);
                 QN[i] = QC[i];
             }
             if constexpr (PBREG) {
 #pragma unroll
-                for (int p = 0; p < P; ++p) { PR[p] = PR[p] + (double)pacc[p]; pacc[p] = R(0); }
+                for (int p = 0; p < P; ++p) {
+                    PR[p] = EXT ? M<double>::fma(h6d, (double)pacc[p], PR[p]) : PR[p] + (double)pacc[p];
+                    pacc[p] = R(0);
+                }
             } else if (STEP_ACC) {
 #pragma unroll
-                for (int p = 0; p < P; ++p) { PB[p] = PB[p] + (double)pacc[p]; pacc[p] = R(0); }
+                for (int p = 0; p < P; ++p) {
+                    PB[p] = EXT ? M<double>::fma(h6d, (double)pacc[p], PB[p]) : PB[p] + (double)pacc[p];
+                    pacc[p] = R(0);
+                }
             }
         }
     }
@@ -862,7 +930,7 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
 #pragma unroll
     for (int i = 0; i < N; ++i) {
         a.dx0[i * B + b] = LAM[i];
-        if (a.phase == 2 && a.kahan) a.lamc[i * B + b] = CL[i];
+        if ((a.phase == 2 && a.kahan) || EXT) a.lamc[i * B + b] = CL[i];
     }
 }
 
@@ -1097,12 +1165,15 @@ __device__ __forceinline__ unsigned pk_warp_max(unsigned v) { return __reduce_ma
 // NSTG: the slice's components of the state (1), and of the stage inputs Y2,
 // Y3, Y4 (4), are also stored to stg + j part ([N][B] each) when `store`: one
 // slot of an adjoint trajectory (as rk4_step).
-template <typename R, bool KAHAN, int NSTG = 0, class SL, class V>
+// EXT: extended-state step (as rk4_step): the slice's part of h f_lo(Q) is
+// evaluated with stage 1, from the same published Q.
+template <typename R, bool KAHAN, int NSTG = 0, bool EXT = false, class SL, class V>
 __device__ __forceinline__ void ws_step(const SL& sl, R* b0, R* b1, V& Q, V& Cm, V& S, V& K, V& Mi, R ua, R ub,
                                         R uc, R h, R h2, R h6, bool act, R* stg = nullptr, long long part = 0,
-                                        long long sB = 0, int b = 0, bool store = false) {
+                                        long long sB = 0, int b = 0, bool store = false, R h6lo = R(0)) {
     typedef M<R> m;
     constexpr int MM = SL::MM;
+    RegVec<R, EXT ? MM : 1> Kc;
 #pragma unroll
     for (int i = 0; i < MM; ++i) Mi[i] = Q[i];   // stage 1 evaluates at Q
     if constexpr (NSTG >= 1) {
@@ -1111,12 +1182,19 @@ __device__ __forceinline__ void ws_step(const SL& sl, R* b0, R* b1, V& Q, V& Cm,
 #pragma unroll(SL::ROLL ? 1 : 4)
     for (int st = 0; st < 4; ++st) {
         const R u = st == 0 ? ua : (st == 3 ? uc : ub);
+        if constexpr (EXT) {
+            if (st == 0) sl.rhs_lo(Mi, b0, u, Kc);
+        }
         sl.rhs(Mi, (st & 1) ? b1 : b0, u, K);
         if (st == 3) {
 #pragma unroll
             for (int i = 0; i < MM; ++i) {
                 const R sum = m::add(S[i], K[i]);
-                if (KAHAN) {
+                if constexpr (EXT) {
+                    R hi = Q[i], lo = Cm[i];
+                    ext_update(hi, lo, sum, Kc[i], h, h6, h6lo);
+                    if (act) { Q[i] = hi; Cm[i] = lo; }
+                } else if (KAHAN) {
                     const R inc = m::mul(h6, sum);
                     const R y = m::sub(inc, Cm[i]);
                     const R t = m::add(Q[i], y);
@@ -1148,7 +1226,7 @@ __device__ __forceinline__ void ws_step(const SL& sl, R* b0, R* b1, V& Q, V& Cm,
 
 // HTRAJ: as fwd_core_iv (1 states after every traj_every-th step, 2 the
 // adjoint trajectory, 3 checkpoints).
-template <typename R, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, int N, class SL, class V>
+template <typename R, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, int N, bool EXT = false, class SL, class V>
 __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const Forcing<R>& frc, R* sm, int b,
                                         bool out, const RunCtx& rc, unsigned T, V& Q, V& Cm, V& Mx, R& sq,
                                         R& sqc) {
@@ -1182,11 +1260,12 @@ __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const
             }
         }
         if constexpr (HTRAJ == 2)
-            ws_step<R, KAHAN, adj_slot_vecs<R>()>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act,
-                                                  a.traj + (long long)(step - a.step0) * adj_slot_vecs<R>() * N * B,
-                                                  (long long)N * B, B, b, out && act);
+            ws_step<R, KAHAN, adj_slot_vecs<R>(), EXT>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act,
+                                                       a.traj + (long long)(step - a.step0) * adj_slot_vecs<R>() * N * B,
+                                                       (long long)N * B, B, b, out && act, a.h6lo);
         else
-            ws_step<R, KAHAN>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act);
+            ws_step<R, KAHAN, 0, EXT>(sl, b0, b1, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, act, nullptr, 0, 0, 0,
+                                      false, a.h6lo);
         if (act) {
             if (HTRAJ == 1 && out) {
                 const long long slot = traj_slot(step, a.step0, a.traj_every);
@@ -1201,7 +1280,7 @@ __device__ __forceinline__ void ws_core(const SL& sl, const FwdArgs<R>& a, const
 // Batch forward (FwdArgs): lane b of every warp of the block; `valid` is false
 // for the lanes past the batch, which run a copy of the last system and store
 // nothing.
-template <typename R, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, int N, class SL>
+template <typename R, bool KAHAN, bool HMAX, bool HSQ, int HTRAJ, int N, bool EXT = false, class SL>
 __device__ __forceinline__ void ws_fwd(SL& sl, const FwdArgs<R>& a, R* sm, int b, bool valid) {
     typedef RegVec<R, SL::MM> V;
     const long long B = a.B;
@@ -1218,9 +1297,11 @@ __device__ __forceinline__ void ws_fwd(SL& sl, const FwdArgs<R>& a, R* sm, int b
     rc.nsteps = (unsigned)a.nsteps;
     rc.max_start = a.max_start;
     rc.sq_start = a.sq_start;
-    ws_core<R, KAHAN, HMAX, HSQ, HTRAJ, N>(sl, a, a.frc, sm, b, valid, rc, (unsigned)a.nsteps, Q, Cm, Mx, sq, sqc);
+    ws_core<R, KAHAN, HMAX, HSQ, HTRAJ, N, EXT>(sl, a, a.frc, sm, b, valid, rc, (unsigned)a.nsteps, Q, Cm, Mx, sq,
+                                                sqc);
     if (!valid) return;
     sl.store_vec(Q, a.state, B, b);
+    if (EXT && a.comp_out) sl.store_vec(Cm, a.comp_out, B, b);
     if (HTRAJ == 2) sl.store_vec(Q, a.traj + (long long)a.nsteps * adj_slot_vecs<R>() * N * B, B, b);
     if (HMAX) sl.store_max(Mx, a.out_max, B, b);
     if (HSQ && SL::SQOWN) a.out_sq[b] = sq;
@@ -1288,7 +1369,7 @@ __device__ __forceinline__ void ws_pool(SL& sl, const PoolArgs<R>& p, R* sm, int
 // of GenSys::vjp; the owner of destination i accumulates the gradients of the
 // values of i's terms (PO of them: FP64 totals, STEP_ACC: per-step FP32 sums
 // first).
-template <typename R, bool KAHAN, bool HSQ, bool STEP_ACC, int N, class SL>
+template <typename R, bool KAHAN, bool HSQ, bool STEP_ACC, int N, bool EXT = false, class SL>
 __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b, bool valid) {
     typedef M<R> m;
     typedef RegVec<R, SL::MM> V;
@@ -1321,8 +1402,11 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                 if (valid) sl.zero_pbar(a.pbar, B, b);
             }
             sl.load_vec(Q, a.x0, B, b);
+            if constexpr (EXT) sl.load_vec(Cm, a.x0 + (long long)N * B, B, b);   // the low parts of x0
+            else {
 #pragma unroll
-            for (int i = 0; i < MM; ++i) Cm[i] = R(0);
+                for (int i = 0; i < MM; ++i) Cm[i] = R(0);
+            }
         } else {
             const R* ck = a.ckpt + (long long)(t0 / a.C) * 2 * N * B;
             sl.load_vec(Q, ck, B, b);
@@ -1340,7 +1424,8 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             const R ua = force_at(a.frc, ebase, st, 0u, 0u);
             const R ub = force_at(a.frc, ebase, st, 0u, 1u);
             const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-            ws_step<R, KAHAN>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true);
+            ws_step<R, KAHAN, 0, EXT>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true, nullptr, 0, 0, 0,
+                                      false, a.h6lo);
         }
         if (a.phase == 1) {   // the next segment starts from this checkpoint
             if (valid && t1 < a.nsteps && t1 % a.C == 0) {
@@ -1374,6 +1459,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
         if constexpr (PBREG) sl.load_pbar(PB, a.pbar, B, b);
     }
     const R gsq2h = a.g_sq ? m::mul(m::mul(a.g_sq[b], R(2)), a.h) : R(0);
+    const double h6d = (double)a.h6 + (double)a.h6lo;   // h/6 (extended-state mode)
     for (int k = khi; k >= klo; --k) {
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
@@ -1389,8 +1475,9 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                 const R ua = force_at(a.frc, ebase, st, 0u, 0u);
                 const R ub = force_at(a.frc, ebase, st, 0u, 1u);
                 const R uc = force_at(a.frc, ebase, st, 1u, 0u);
-                ws_step<R, KAHAN, SV>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true,
-                                      a.buf + (long long)(t - start) * SV * N * B, (long long)N * B, B, b, valid);
+                ws_step<R, KAHAN, SV, EXT>(sl, rq, r2, Q, Cm, S, K, Mi, ua, ub, uc, a.h, a.h2, a.h6, true,
+                                           a.buf + (long long)(t - start) * SV * N * B, (long long)N * B, B, b, valid,
+                                           a.h6lo);
             }
         } else {
             sl.load_vec(Q, a.buf + (long long)(end - slot0) * SV * N * B, B, b);
@@ -1433,7 +1520,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             } else {
                 load_slot(t, QC, Y2, Y3, Y4);
             }
-            if (HSQ && a.g_sq && t >= a.sq_start) sl.template add_sq_grad<KAHAN>(LAM, CL, QN, gsq2h);
+            if (HSQ && a.g_sq && t >= a.sq_start) sl.template add_sq_grad<KAHAN, EXT>(LAM, CL, QN, gsq2h);
             // the forcing of step t, read one step ahead (uc of step t-1 is ua of step t)
             const R ua = fa, ub = fb, uc = fc;
             if (t > start) {
@@ -1443,7 +1530,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             }
 #pragma unroll
             for (int i = 0; i < MM; ++i) {
-                KB[i] = m::mul(a.h6, LAM[i]);
+                KB[i] = EXT ? LAM[i] : m::mul(a.h6, LAM[i]);   // extended-state mode: no h/6 (see adj_run_jit)
                 QB[i] = KAHAN ? R(0) : LAM[i];   // the step's increment (Kahan) or LAM + it
             }
             V Yc;
@@ -1485,6 +1572,9 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                     pk_block_sync();
                 }
             }
+            // extended-state mode: h J_lo(QC)^T LAM, from QC (rq) and LAM (= KB, k0)
+            V YC;
+            if constexpr (EXT) sl.vjp_lo(QC, rq, KB, k0, ua, YC);
             // reverse sweep: VJPs at Y4, Y3, Y2, QC with weights from k0, k1, k0, k1
 #pragma unroll(SL::ROLL ? 1 : 4)
             for (int st = 0; st < 4; ++st) {
@@ -1506,7 +1596,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                 const R c = st == 0 ? a.h : a.h2;
 #pragma unroll
                 for (int i = 0; i < MM; ++i) {
-                    const R sb = m::mul(a.h6, LAM[i]);
+                    const R sb = EXT ? LAM[i] : m::mul(a.h6, LAM[i]);
                     QB[i] = m::add(QB[i], YB[i]);
                     KB[i] = m::fma(c, YB[i], st < 2 ? m::mul(R(2), sb) : sb);
                 }
@@ -1515,16 +1605,18 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             }
 #pragma unroll
             for (int i = 0; i < MM; ++i) {
-                if (KAHAN) kahan_add(LAM[i], CL[i], m::add(QB[i], YB[i]));
+                if constexpr (EXT) ext_update(LAM[i], CL[i], m::add(QB[i], YB[i]), YC[i], a.h, a.h6, a.h6lo);
+                else if (KAHAN) kahan_add(LAM[i], CL[i], m::add(QB[i], YB[i]));
                 else LAM[i] = m::add(QB[i], YB[i]);
                 QN[i] = QC[i];
             }
             if constexpr (STEP_ACC) {
                 if constexpr (PBREG) {
 #pragma unroll
-                    for (int p = 0; p < PO; ++p) PB[p] = PB[p] + (double)pst[p];
+                    for (int p = 0; p < PO; ++p)
+                        PB[p] = EXT ? M<double>::fma(h6d, (double)pst[p], PB[p]) : PB[p] + (double)pst[p];
                 } else {
-                    if (valid) sl.add_pbar(pst, a.pbar, B, b);
+                    if (valid) sl.template add_pbar<EXT>(pst, a.pbar, B, b, h6d);
                 }
 #pragma unroll
                 for (int p = 0; p < PO; ++p) pst[p] = R(0);
@@ -1534,7 +1626,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     }
     if (!valid) return;
     sl.store_vec(LAM, a.dx0, B, b);
-    if (KAHAN && a.phase == 2) sl.store_vec(CL, a.lamc, B, b);
+    if ((KAHAN && a.phase == 2) || EXT) sl.store_vec(CL, a.lamc, B, b);
     if constexpr (PBREG) sl.store_pbar(PB, a.pbar, B, b);
 }
 

@@ -25,7 +25,7 @@ def main(argv=None):
     ap.add_argument("--config", default="coupled2", choices=sorted(synth.CONFIGS))
     ap.add_argument("--systems", type=int, default=None)
     ap.add_argument("--nsteps", type=int, default=None)
-    ap.add_argument("--precision", default="fp32_kahan", choices=["fp64", "fp32", "fp32_kahan"])
+    ap.add_argument("--precision", default="fp32_kahan", choices=["fp64", "fp32", "fp32_kahan", "fp32_ext"])
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--generic", action="store_true", help="use the pattern-interpreting kernel")
     ap.add_argument("--adjoint", action="store_true", help="run the exact adjoint (gradients) instead")

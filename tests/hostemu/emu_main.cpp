@@ -210,9 +210,15 @@ int main(int argc, char** argv) {
     const int nsteps = std::atoi(argv[9]);
     const double h = std::atof(argv[10]);
     typedef pk::R R;
-    auto vals = readf<R>(dir, "vals.bin", (size_t)P * B);
-    auto state = readf<R>(dir, "x0.bin", (size_t)n * B);
+    // EMU_EXT=1: extended-state mode, vals.bin [2P][B] and x0.bin [2n][B]
+    // (high parts, then low parts); out.bin [2n][B]
+    const char* ext_env = std::getenv("EMU_EXT");
+    const int ext = ext_env ? std::atoi(ext_env) : 0;
+    const size_t np = ext ? 2 : 1;
+    auto vals = readf<R>(dir, "vals.bin", (size_t)P * B * np);
+    auto state = readf<R>(dir, "x0.bin", (size_t)n * B * np);
     auto exc = readf<int>(dir, "exc.bin", (size_t)B);
+    const R h6lo = (R)(h / 6.0 - (double)(R)(h / 6.0));
     auto x = readf<R>(dir, "x.bin", (size_t)n_exc * len);
     auto im = readf<R>(dir, "im.bin", (size_t)2 * W);
     pk::Forcing<R> frc;
@@ -239,6 +245,11 @@ int main(int argc, char** argv) {
     a.B = B;
     a.step0 = step0;
     a.nsteps = nsteps;
+    if (ext) {
+        a.comp = state.data() + (size_t)n * B;
+        a.comp_out = state.data() + (size_t)n * B;
+        a.h6lo = h6lo;
+    }
     for (int b = 0; b < B; ++b) emu_launch(b, [&] { pk_fwd(a); });
     std::snprintf(path, sizeof path, "%s/out.bin", dir);
     FILE* f = std::fopen(path, "wb");
@@ -273,7 +284,9 @@ int main(int argc, char** argv) {
     a.nsteps = nsteps;
     a.C = C;
     a.nck = nck;
-    a.kahan = kahan;
+    a.kahan = kahan || ext;
+    a.ext = ext;
+    a.h6lo = ext ? h6lo : R(0);
     a.sq_start = sq_start;
     std::vector<R> lamc((size_t)B * n, R(0));
     a.lamc = lamc.data();
@@ -326,6 +339,10 @@ int main(int argc, char** argv) {
     std::snprintf(path, sizeof path, "%s/dx0.bin", dir);
     f = std::fopen(path, "wb");
     std::fwrite(dx0.data(), sizeof(R), dx0.size(), f);
+    std::fclose(f);
+    std::snprintf(path, sizeof path, "%s/lamc.bin", dir);   // low parts of dx0 (extended-state mode)
+    f = std::fopen(path, "wb");
+    std::fwrite(lamc.data(), sizeof(R), lamc.size(), f);
     std::fclose(f);
 #endif
     return 0;

@@ -42,16 +42,29 @@ def build_emulator(d, src, define=None):
     return exe, env
 
 
+def hi_lo(a):
+    """[B][k] FP64 -> [B][2k] FP32: high parts, then the low parts (the
+    extended-state mode's split of values and initial states)."""
+    a = np.asarray(a, np.float64)
+    hi = a.astype(np.float32)
+    return np.concatenate([hi, (a - hi.astype(np.float64)).astype(np.float32)], axis=1)
+
+
 def run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, h, step0, nsteps, prec, slicing=None):
     src = Plan(pat, prec, slicing=slicing).jit_report(vals, window=W, im=im).split("// ---- source ----\n", 1)[1]
     default_sliced = pat.n >= 28 if prec != "fp64" else pat.n >= 8 or (pat.n >= 3 and len(vals) <= 8192)
+    if prec == "fp32_ext":   # fewer components per warp: sliced from n >= 28 as well
+        default_sliced = pat.n >= 28
     assert ("warp-sliced" in src) == (bool(slicing) or (slicing is None and default_sliced))
     d = str(tmp_path)
     exe, env = build_emulator(d, src)
     dt = np.float64 if prec == "fp64" else np.float32
     B = vals.shape[0]
-    np.ascontiguousarray(vals.T.astype(dt)).tofile(os.path.join(d, "vals.bin"))
-    np.ascontiguousarray(x0.T.astype(dt)).tofile(os.path.join(d, "x0.bin"))
+    ext = prec == "fp32_ext"
+    if ext:
+        env["EMU_EXT"] = "1"
+    np.ascontiguousarray((hi_lo(vals) if ext else vals).T.astype(dt)).tofile(os.path.join(d, "vals.bin"))
+    np.ascontiguousarray((hi_lo(x0) if ext else x0).T.astype(dt)).tofile(os.path.join(d, "x0.bin"))
     np.asarray(exc, np.int32).tofile(os.path.join(d, "exc.bin"))
     np.asarray(x, dt).tofile(os.path.join(d, "x.bin"))
     (np.asarray(im, dt).reshape(-1) if W else np.zeros(0, dt)).tofile(os.path.join(d, "im.bin"))
@@ -59,11 +72,15 @@ def run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, h, step0, nsteps, prec,
     r = subprocess.run([exe, d, str(B), str(pat.n), str(pat.P), str(xs.shape[0]), str(xs.shape[1]), str(W),
                         str(step0), str(nsteps), repr(float(h)), "0"], capture_output=True, text=True, env=env)
     assert r.returncode == 0, r.stderr
-    return np.fromfile(os.path.join(d, "out.bin"), dtype=dt).reshape(pat.n, B).T.astype(np.float64)
+    out = np.fromfile(os.path.join(d, "out.bin"), dtype=dt).astype(np.float64)
+    if ext:   # high + low parts
+        out = out.reshape(2, pat.n, B)
+        return (out[0] + out[1]).T
+    return out.reshape(pat.n, B).T
 
 
 @pytest.mark.parametrize("slicing", [False, True])
-@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan", "fp32_ext"])
 @pytest.mark.parametrize("seed,W,step0,nsteps", [(0, 8, 3, 61), (1, 0, 0, 40), (2, 4, 1, 30), (3, 2, 0, 25)])
 def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps, slicing):
     rng = np.random.default_rng(500 + seed)
@@ -97,8 +114,11 @@ def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N,
         env["EMU_ADJ_STORED"] = "1"
     dt = np.float64 if prec == "fp64" else np.float32
     B = len(vals)
-    np.ascontiguousarray(vals.T, dt).tofile(os.path.join(d, "vals.bin"))
-    np.ascontiguousarray(x0.T, dt).tofile(os.path.join(d, "x0.bin"))
+    ext = prec == "fp32_ext"
+    if ext:
+        env["EMU_EXT"] = "1"
+    np.ascontiguousarray((hi_lo(vals) if ext else vals).T, dt).tofile(os.path.join(d, "vals.bin"))
+    np.ascontiguousarray((hi_lo(x0) if ext else x0).T, dt).tofile(os.path.join(d, "x0.bin"))
     np.asarray(exc, np.int32).tofile(os.path.join(d, "exc.bin"))
     np.asarray(x, dt).tofile(os.path.join(d, "x.bin"))
     np.ascontiguousarray(gs, dt).tofile(os.path.join(d, "gsq.bin"))
@@ -110,6 +130,8 @@ def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N,
     assert r.returncode == 0, r.stderr
     pbar = np.fromfile(os.path.join(d, "pbar.bin")).reshape(pat.P, B).T
     dx0 = np.fromfile(os.path.join(d, "dx0.bin"), dtype=dt).reshape(pat.n, B).T.astype(np.float64)
+    if ext:   # high + low parts of the adjoint state
+        dx0 = dx0 + np.fromfile(os.path.join(d, "lamc.bin"), dtype=dt).reshape(pat.n, B).T.astype(np.float64)
     return pbar, dx0
 
 
@@ -143,8 +165,9 @@ def test_generated_adjoint_matches_oracle(tmp_path, seed, slicing):
     np.testing.assert_array_equal(dx0, odx)
 
 
+@pytest.mark.parametrize("prec", ["fp32_kahan", "fp32_ext"])
 @pytest.mark.parametrize("seed", range(3))
-def test_generated_adjoint_fp32_sliced_equals_thread(tmp_path, seed):
+def test_generated_adjoint_fp32_sliced_equals_thread(tmp_path, seed, prec):
     """FP32 adjoint (per-step FP32 gradient sums into FP64 totals): the warp-
     sliced kernel equals the thread-per-system kernel bit for bit."""
     pat, vals, x0, exc, x, im, gf, gs, N, sq = _adjoint_case(seed)
@@ -154,14 +177,14 @@ def test_generated_adjoint_fp32_sliced_equals_thread(tmp_path, seed):
     for slicing in (False, True):
         d = os.path.join(str(tmp_path), str(slicing))
         os.makedirs(d)
-        out.append(run_emulated_adjoint(d, pat, "fp32_kahan", slicing, vals, x0, exc, x, im, gf, gs, N, sq, N // 3))
+        out.append(run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, N // 3))
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
 
 
 @pytest.mark.parametrize("split", [0, 2])
 @pytest.mark.parametrize("prec,slicing", [("fp64", False), ("fp64", True), ("fp32_kahan", False),
-                                          ("fp32_kahan", True)])
+                                          ("fp32_kahan", True), ("fp32_ext", False), ("fp32_ext", True)])
 def test_generated_adjoint_stored_equals_checkpointed(tmp_path, prec, slicing, split):
     """The backward sweep over a stored trajectory (one forward pass) gives
     the bits of the checkpointed adjoint (forward pass, then per-chunk
@@ -264,13 +287,13 @@ def test_generated_pool_matches_oracle(tmp_path, prec, seed, W, slicing):
         k += m
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan", "fp32_ext"])
 def test_generated_warp_sliced_banded32(tmp_path, prec):
     """64-state banded system: the default kernel is warp-sliced (8 warps,
     components crossing warps through shared memory); equals the oracle."""
     w = synth.banded32(n_sys=6, nsteps=150, sig_len=256)
     got = run_emulated(tmp_path, w.pattern, w.values, w.x0, w.exc_index, w.signals, w.window, w.im, w.h, 0,
-                       w.nsteps, prec, slicing=None if prec == "fp32_kahan" else True)
+                       w.nsteps, prec, slicing=None if prec != "fp64" else True)
     ref, _, _ = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
                                 prec)
     np.testing.assert_array_equal(got, ref)
@@ -298,7 +321,7 @@ def test_generated_adjoint_banded32_default_slices(tmp_path):
     assert np.abs(out[0][0]).max() > 0
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32_kahan", "fp32_ext"])
 @pytest.mark.parametrize("slicing", [False, True])
 @pytest.mark.parametrize("split", [1, 2])
 def test_generated_adjoint_split_launches(tmp_path, prec, slicing, split):

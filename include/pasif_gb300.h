@@ -59,6 +59,13 @@ extern "C" {
                                        size (default: from n >= 28 in FP32,
                                        n >= 24 in FP64)                     */
 #define PASIF_PLAN_NO_WARP_SLICED 8 /* plan flag: thread per system always  */
+#define PASIF_PLAN_FAST 16          /* plan flag: fast thread-per-system
+                                       forward kernels (products of the state
+                                       shared between terms, the RK sum and
+                                       the compensation folded into fmas):
+                                       not the oracle's bit-exact operation
+                                       order; accuracy as checked against
+                                       FP64.  No reference counterpart      */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* pasif_last_error(void);
@@ -156,6 +163,20 @@ int pasif_driver_get_gradient(pasif_driver* d, unsigned save, double* out, long 
                               long long* out_len);
 /* Kernel used by the last forward solve (PASIF_KERNEL_*). */
 int pasif_driver_last_kernel(pasif_driver* d, int* kind);
+/* Memory-bounded sweeps: the reference splits its excitation copies into
+ * sequential chunks that fit the free device memory
+ * (numberOfSimulationToPerform, src/__GpuDriver.cu:420-449, 896-938; its
+ * chunks read the wrong excitation offset).  Here every instance (block x
+ * signal) keeps its own signal, and a solve whose instances need more device
+ * memory than the budget runs as sequential batches of as many instances as
+ * fit.  bytes = 0 (default): 90 % of the memory free when the solve starts.
+ * A solve in which not even one instance fits returns PASIF_ERR_MEMORY. */
+int pasif_driver_set_memory_budget(pasif_driver* d, long long bytes);
+/* Sequential batches the last solve of this driver ran (1: all at once). */
+int pasif_driver_last_chunks(pasif_driver* d, int* chunks);
+/* The split rule itself: instances per sequential batch for n_instances of
+ * bytes_per_instance within budget (all when they fit; 0 when none fits). */
+int pasif_sweep_chunk(long long n_instances, long long bytes_per_instance, long long budget, long long* per_batch);
 
 /* ======================================================================
  * Layer 2: native batches

@@ -168,3 +168,16 @@ class __GpuDriver:
         k = C.c_int()
         N.check(N.lib.pasif_driver_last_kernel(self._pasif_handle, C.byref(k)))
         return {0: "none", 1: "generic", 2: "specialised"}[k.value]
+
+    # ---- memory-bounded sweeps (no reference method: the reference always
+    # splits by the free device memory, src/__GpuDriver.cu:420-449) ----
+    def _setMemoryBudget(self, bytes_: int) -> None:
+        """Device memory a solve may use (0: 90 % of what is free); sweeps
+        beyond it run as sequential batches, each instance on its own signal."""
+        N.check(N.lib.pasif_driver_set_memory_budget(self._pasif_handle, int(bytes_)))
+
+    def _lastChunks(self) -> int:
+        """Sequential batches the last solve ran."""
+        k = C.c_int()
+        N.check(N.lib.pasif_driver_last_chunks(self._pasif_handle, C.byref(k)))
+        return k.value

@@ -7,14 +7,21 @@ drop-in (PASIfgpu), an exact discrete adjoint behind torch.autograd
 """
 from __future__ import annotations
 
-import os
 import sys
 
-from . import _native
-from .batch import Batch, Plan, Signals, forward
 from .system import Pattern, reducers_c
 
 __all__ = ["Pattern", "Plan", "Signals", "Batch", "forward", "install_dropin", "reducers_c"]
+
+
+def __getattr__(name):
+    """The batch interface (and with it libpasif_gb300.so) is loaded on first
+    use: importing the package for its pattern or synthetic-workload helpers
+    maps no native library."""
+    if name in ("Batch", "Plan", "Signals", "forward"):
+        from . import batch
+        return getattr(batch, name)
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")
 
 
 def install_dropin() -> None:

@@ -29,6 +29,7 @@ PLAN_GENERIC_ONLY = 1
 PLAN_NO_LITERALS = 2
 PLAN_WARP_SLICED = 4
 PLAN_NO_WARP_SLICED = 8
+PLAN_FAST = 16
 
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp32_kahan": FP32_KAHAN, "fp32_ext": FP32_EXT}
 
@@ -133,6 +134,9 @@ _SIGS = {
     "pasif_forward_noalloc": (C.c_int, [C.POINTER(PatternC), C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int,
                                         _vp, C.c_double, C.c_int, C.c_int, _vp, _vp]),
     "pasif_forward_noalloc_status": (C.c_int, [_ip, _ip, _vp]),
+    "pasif_driver_set_memory_budget": (C.c_int, [_vp, C.c_longlong]),
+    "pasif_driver_last_chunks": (C.c_int, [_vp, _ip]),
+    "pasif_sweep_chunk": (C.c_int, [C.c_longlong, C.c_longlong, C.c_longlong, _llp]),
     "pasif_forward": (C.c_int, [C.POINTER(PatternC), C.c_int, C.c_int, _dp, _dp, _ip, _dp, C.c_int, C.c_int,
                                 C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.POINTER(ReducersC), _dp, _dp, _dp]),
 }

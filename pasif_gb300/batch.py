@@ -30,13 +30,16 @@ def _stream(stream) -> C.c_void_p:
 
 class Plan:
     def __init__(self, pattern: Pattern, precision="fp64", generic_only: bool = False, literals: bool = True,
-                 slicing=None):
+                 slicing=None, fast: bool = False):
         """literals=False: the specialised kernels load every value, so one
         compiled kernel serves every batch of the plan (serving).
         slicing: None = warp-sliced kernels where they are faster on GB300
         (forward: FP32 from n >= 28, FP64 from n >= 8, or n >= 3 for batches
         up to 8192 systems; adjoint: FP32 from n >= 5, FP64 from n >= 2),
-        True = always, False = never (thread per system)."""
+        True = always, False = never (thread per system).
+        fast=True: the fast thread-per-system forward kernels (shared state
+        products, folded RK sum): results differ from the oracle's bits and
+        are checked against FP64 instead."""
         self.pattern = pattern
         self.precision = _prec(precision)
         self._c = pattern.to_c()
@@ -44,6 +47,8 @@ class Plan:
         flags = (N.PLAN_GENERIC_ONLY if generic_only else 0) | (0 if literals else N.PLAN_NO_LITERALS)
         if slicing is not None:
             flags |= N.PLAN_WARP_SLICED if slicing else N.PLAN_NO_WARP_SLICED
+        if fast:
+            flags |= N.PLAN_FAST
         N.check(N.lib.pasif_plan_create(C.byref(h), C.byref(self._c), self.precision, flags))
         self.handle = h
 
@@ -253,3 +258,52 @@ def forward(pattern: Pattern, values, x0, exc_index, x, h: float, nsteps: int, w
                                 xa.shape[0], xa.shape[1], int(window), N.dptr(im_a) if im_a is not None else None,
                                 float(h), int(step0), int(nsteps), C.byref(red), N.dptr(st), N.dptr(mx), N.dptr(sq)))
     return st, mx[:, :int(red.n_max)], sq
+
+
+def verified_adjoint(pattern: Pattern, values, x0, exc_index, x, h: float, nsteps: int, window: int = 0, im=None,
+                     g_final=None, g_sq=None, sq_comp=(), sq_start: int = 0, tol: float = 5e-6,
+                     adjoint_storage=None, stream=None):
+    """Gradients for every system within about 1e-5 of FP64, at FP32 speed
+    for the systems FP32 stage arithmetic can serve.
+
+    The extended-state adjoint ("fp32_ext") of every system is cross-checked
+    against the compensated-FP32 adjoint ("fp32_kahan"): both carry the
+    FP32 rounding of the stages, through different update arithmetic, so on
+    a system whose trajectory amplifies rounding (chaotic or near-resonant
+    over the horizon) they disagree.  Systems whose gradients differ by more
+    than `tol` (per system, max|g_ext - g_kahan| / max|g_ext|) are recomputed
+    with the FP64 adjoint.  On the 8-DOF chain configuration (4096 systems x
+    5e4 steps) tol = 5e-6 flags 2 % of the systems, every one whose
+    extended-state error exceeds 1e-5 among them (GB300 measurement).
+
+    Returns (d_values[n_sys][P], d_x0[n_sys][n], recomputed indices)."""
+    v = N.f64(values).reshape(-1, pattern.P)
+    n_sys = v.shape[0]
+    x0a = N.f64(x0).reshape(n_sys, pattern.n)
+    e = N.i32(exc_index).reshape(n_sys)
+    gf = N.f64(g_final).reshape(n_sys, pattern.n) if g_final is not None else None
+    gs = N.f64(g_sq).reshape(n_sys) if g_sq is not None else None
+    out = {}
+    for prec in ("fp32_ext", "fp32_kahan"):
+        b = Batch(Plan(pattern, prec), v, x0a, e, stream=stream)
+        if adjoint_storage is not None:
+            b.adjoint_storage(adjoint_storage)
+        out[prec] = b.adjoint(Signals(x, window, im, prec, stream=stream), h, nsteps, gf, gs, sq_comp, sq_start,
+                              stream=stream)
+        del b
+    dv, dx = out["fp32_ext"]
+    dk = out["fp32_kahan"][0]
+    scale = np.maximum(np.max(np.abs(dv), axis=1), 1e-300)
+    redo = np.where(np.max(np.abs(dv - dk), axis=1) / scale > tol)[0]
+    if redo.size:
+        b = Batch(Plan(pattern, "fp64"), v[redo], x0a[redo], e[redo], stream=stream)
+        if adjoint_storage is not None:
+            b.adjoint_storage(adjoint_storage)
+        rv, rx = b.adjoint(Signals(x, window, im, "fp64", stream=stream), h, nsteps,
+                           gf[redo] if gf is not None else None, gs[redo] if gs is not None else None, sq_comp,
+                           sq_start, stream=stream)
+        dv = dv.copy()
+        dx = dx.copy()
+        dv[redo] = rv
+        dx[redo] = rx
+    return dv, dx, redo

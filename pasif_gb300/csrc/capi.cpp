@@ -290,6 +290,26 @@ int pasif_driver_get_gradient(pasif_driver* d, unsigned save, double* out, long 
     });
 }
 
+int pasif_driver_set_memory_budget(pasif_driver* d, long long bytes) {
+    DRV_CHECK(d);
+    std::string err;
+    return done(d->d->set_memory_budget(bytes, &err), err);
+}
+
+int pasif_driver_last_chunks(pasif_driver* d, int* chunks) {
+    DRV_CHECK(d);
+    if (!chunks) return fail(PASIF_ERR_INVALID, "null output");
+    *chunks = d->d->last_chunks();
+    return PASIF_OK;
+}
+
+int pasif_sweep_chunk(long long n_instances, long long bytes_per_instance, long long budget, long long* per_batch) {
+    if (!per_batch || n_instances < 0 || bytes_per_instance < 0 || budget < 0)
+        return fail(PASIF_ERR_INVALID, "negative size or null output");
+    *per_batch = pasif::sweep_chunk(n_instances, bytes_per_instance, budget);
+    return PASIF_OK;
+}
+
 int pasif_driver_last_kernel(pasif_driver* d, int* kind) {
     DRV_CHECK(d);
     if (!kind) return fail(PASIF_ERR_INVALID, "null output");
@@ -310,6 +330,7 @@ int pasif_plan_create(pasif_plan** out, const pasif_pattern* pattern, int precis
         if (rc) return fail(rc, err);
         h->p->no_literals = (flags & PASIF_PLAN_NO_LITERALS) != 0;
         h->p->slicing = (flags & PASIF_PLAN_WARP_SLICED) ? 1 : (flags & PASIF_PLAN_NO_WARP_SLICED) ? -1 : 0;
+        h->p->fast = (flags & PASIF_PLAN_FAST) != 0;
         *out = h.release();
         return PASIF_OK;
     });
@@ -596,6 +617,7 @@ int pasif_plan_jit_report(const pasif_plan* p, const double* values, int n_sys, 
         key.max_mask = max_mask;
         key.sq_mask = sq_mask;
         key.slices = p->p->slicing < 0 ? 0 : pasif::ws_slices(p->p->pat, f32, p->p->slicing > 0, n_sys, key.ext);
+        key.fast = p->p->fast && !key.ext && key.slices < 2;
         if (window < 0 || (window > 0 && (!im || (window & (window - 1)))))
             return fail(PASIF_ERR_INVALID, "window must be 0 or a power of two with weights");
         key.window = window;

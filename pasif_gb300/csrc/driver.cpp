@@ -11,6 +11,7 @@
 // results are those of the canonical order the oracle fixes.
 #include "driver.h"
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -228,6 +229,31 @@ int Driver::load_excitations(const double* const* sig, const long long* len, int
     return 0;
 }
 
+long long sweep_chunk(long long n_instances, long long bytes_per_instance, long long budget) {
+    if (n_instances <= 0) return 0;
+    if (bytes_per_instance <= 0) return n_instances;
+    const long long fit = budget / bytes_per_instance;
+    return fit >= n_instances ? n_instances : fit;
+}
+
+int Driver::set_memory_budget(long long bytes, std::string* err) {
+    if (bytes < 0) { *err = "negative memory budget"; return 1; }
+    mem_budget_ = bytes;
+    return 0;
+}
+
+// The budget of a solve: the set one, or 90 % of the free device memory plus
+// `held` bytes the driver's own buffers for this solve already occupy.
+long long Driver::budget_for(long long held) const {
+    if (mem_budget_ > 0) return mem_budget_;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return 1LL << 62;   // unknown: no split
+    }
+    return (long long)((double)free_b * 0.9) + held;
+}
+
 int Driver::set_precision(int p, std::string* err) {
     if (p < kFP64 || p > kFP32Ext) { *err = "unknown precision"; return 1; }
     if (p != precision_) { precision_ = p; signals_.reset(); groups_.clear(); }
@@ -355,20 +381,18 @@ int Driver::build_forward_groups(std::string* err) {
         rc = plan_create(b0.pat, precision_, false, &g.plan, err);
         if (rc) return rc;
         const int nb = (int)g.blocks.size(), B = nb * E, P = b0.pat.P(), n = b0.pat.n;
-        rc = batch_create(g.plan, B, &g.batch, err);
-        if (rc) return rc;
-        std::vector<double> vals((size_t)B * P), x0((size_t)B * n);
-        std::vector<int> exc(B);
+        g.hvals.assign((size_t)B * P, 0.0);
+        g.hx0.assign((size_t)B * n, 0.0);
+        g.hexc.assign(B, 0);
         for (int e = 0; e < E; ++e)
             for (int c = 0; c < nb; ++c) {
                 const Block& bl = blocks_[g.blocks[c]];
                 const size_t b = (size_t)e * nb + c;
-                for (int q = 0; q < P; ++q) vals[b * P + q] = bl.vals[q];
-                for (int i = 0; i < n; ++i) x0[b * n + i] = fwd_.ic[bl.nodes[i]];
-                exc[b] = e;
+                for (int q = 0; q < P; ++q) g.hvals[b * P + q] = bl.vals[q];
+                for (int i = 0; i < n; ++i) g.hx0[b * n + i] = fwd_.ic[bl.nodes[i]];
+                g.hexc[b] = e;   // the instance's own signal, whatever batch it runs in
             }
-        rc = g.batch->set(vals.data(), x0.data(), exc.data(), kHost, stream_, err);
-        if (rc) return rc;
+        g.resident = 0;   // uploaded by the first solve, in one batch or in sequential ones
     }
     if (dcompute_)
         info(std::to_string(blocks_.size()) + " independent blocks in " + std::to_string(groups_.size()) +
@@ -389,34 +413,68 @@ int Driver::run_forward(int traj_every, long long slots, std::vector<double>* fi
     Reducers none;
     if (dsolver_)
         info("RK4: " + std::to_string(numsteps_) + " steps, h=" + std::to_string(h_));
+    last_chunks_ = 0;
     for (auto& g : groups_) {
-        rc = g.batch->forward(*signals_, h_, 0, (int)numsteps_, none, traj_every, slots, stream_, err);
-        if (rc) return rc;
-        last_kind_ = g.batch->last_kind;
-    }
-    for (auto& g : groups_) {
-        const int nb = (int)g.blocks.size(), B = g.batch->B, n = g.plan->pat.n;
-        if (final_out) {
-            std::vector<double> st((size_t)B * n);
-            rc = g.batch->get(st.data(), nullptr, nullptr, h_, kHost, stream_, err);
-            if (rc) return rc;
-            for (int b = 0; b < B; ++b) {
-                const int e = b / nb, c = b % nb;
-                const Block& bl = blocks_[g.blocks[c]];
-                for (int i = 0; i < n; ++i) (*final_out)[(size_t)e * nf_ + bl.nodes[i]] = st[(size_t)b * n + i];
-            }
+        const int nb = (int)g.blocks.size(), B = nb * E, n = g.plan->pat.n, P = g.plan->pat.P();
+        // device bytes per instance: values, x0 and state (high and low parts
+        // in the extended-state mode), reducer output, trajectory slots,
+        // upload staging and the generic kernel's work vectors
+        const long long rs = precision_ == kFP64 ? 8 : 4, np = precision_ == kFP32Ext ? 2 : 1;
+        const long long wide = std::max(P, n);
+        const long long per = rs * ((long long)P * np + 2LL * n * np + 1 + (long long)n * std::max(0LL, slots) +
+                                    6LL * n) + 8 * wide * (np == 2 ? 3 : 1) + 8;
+        const long long chunk = sweep_chunk(B, per, budget_for(g.batch ? (long long)g.resident * per : 0));
+        if (chunk <= 0) {
+            *err = "one instance needs " + std::to_string(per) + " bytes of device memory, more than the budget";
+            return 4;
         }
-        if (traj_out && slots > 0) {
-            std::vector<double> tr((size_t)slots * B * n);
-            rc = g.batch->get_traj(tr.data(), slots, kHost, stream_, err);
+        const long long nchunk = (B + chunk - 1) / chunk;
+        last_chunks_ += (int)nchunk;
+        if (!g.batch || g.batch->B != (int)chunk || (nchunk > 1 && g.resident)) {
+            g.batch.reset();
+            rc = batch_create(g.plan, (int)chunk, &g.batch, err);
             if (rc) return rc;
-            for (long long s = 0; s < slots; ++s)
-                for (int b = 0; b < B; ++b) {
-                    const int e = b / nb, c = b % nb;
-                    const Block& bl = blocks_[g.blocks[c]];
-                    for (int i = 0; i < n; ++i)
-                        (*traj_out)[((size_t)s * E + e) * nf_ + bl.nodes[i]] = tr[((size_t)s * B + b) * n + i];
+            g.resident = 0;
+        }
+        for (long long c0 = 0; c0 < B; c0 += chunk) {
+            const int m = (int)std::min<long long>(chunk, B - c0);
+            if (nchunk > 1 || !g.resident) {   // one resident batch keeps its inputs between solves
+                if (g.batch->B != m) {
+                    rc = g.batch->resize(m, err);
+                    if (rc) return rc;
                 }
+                rc = g.batch->set(g.hvals.data() + c0 * P, g.hx0.data() + c0 * n, g.hexc.data() + c0, kHost,
+                                  stream_, err);
+                if (rc) return rc;
+                g.resident = nchunk == 1 ? m : 0;
+            }
+            rc = g.batch->forward(*signals_, h_, 0, (int)numsteps_, none, traj_every, slots, stream_, err);
+            if (rc) return rc;
+            last_kind_ = g.batch->last_kind;
+            if (final_out) {
+                std::vector<double> st((size_t)m * n);
+                rc = g.batch->get(st.data(), nullptr, nullptr, h_, kHost, stream_, err);
+                if (rc) return rc;
+                for (int k = 0; k < m; ++k) {
+                    const long long b = c0 + k;
+                    const int e = (int)(b / nb), c = (int)(b % nb);
+                    const Block& bl = blocks_[g.blocks[c]];
+                    for (int i = 0; i < n; ++i) (*final_out)[(size_t)e * nf_ + bl.nodes[i]] = st[(size_t)k * n + i];
+                }
+            }
+            if (traj_out && slots > 0) {
+                std::vector<double> tr((size_t)slots * m * n);
+                rc = g.batch->get_traj(tr.data(), slots, kHost, stream_, err);
+                if (rc) return rc;
+                for (long long s = 0; s < slots; ++s)
+                    for (int k = 0; k < m; ++k) {
+                        const long long b = c0 + k;
+                        const int e = (int)(b / nb), c = (int)(b % nb);
+                        const Block& bl = blocks_[g.blocks[c]];
+                        for (int i = 0; i < n; ++i)
+                            (*traj_out)[((size_t)s * E + e) * nf_ + bl.nodes[i]] = tr[((size_t)s * m + k) * n + i];
+                    }
+            }
         }
     }
     return 0;
@@ -450,6 +508,7 @@ int Driver::gradient(unsigned save, std::vector<double>* out, std::string* err) 
         groups[blocks[bi].pat.key() + "#" + blocks[bi].apat.key()].push_back(bi);
     const int E = n_exc_;
     std::vector<double> res((size_t)E * na_, 0.0);
+    last_chunks_ = 0;
     for (auto& kv : groups) {
         const std::vector<int>& ids = kv.second;
         const Block& b0 = blocks[ids[0]];
@@ -482,9 +541,25 @@ int Driver::gradient(unsigned save, std::vector<double>* out, std::string* err) 
             for (double v : a0) std::printf(" %.17g", v);
             std::printf("\n");
         }
-        rc = refgrad_run(*fp, *bp, B, fv.data(), bv.data(), x0.data(), a0.data(), exc.data(), *signals_, h_,
-                         (int)numsteps_, (int)save, o.data(), stream_, err);
-        if (rc) return rc;
+        // device bytes per instance of _getGradient: the slot buffer, the
+        // generic kernel's work vectors, values, states and output
+        const long long rs = precision_ == kFP64 ? 8 : 4;
+        const long long N = numsteps_, S = (long long)std::sqrt((double)N);
+        const long long Cc = S > 0 ? (N + S - 1) / S : 1;
+        const long long per = rs * ((S + Cc - 1) * nf + 5LL * nf + 6LL * na + Pf + Pb + nf + 2LL * na) + 8 * 4 + 4;
+        const long long chunk = sweep_chunk(B, per, budget_for(0));
+        if (chunk <= 0) {
+            *err = "one instance needs " + std::to_string(per) + " bytes of device memory, more than the budget";
+            return 4;
+        }
+        last_chunks_ += (int)((B + chunk - 1) / chunk);
+        for (long long c0 = 0; c0 < B; c0 += chunk) {
+            const int m = (int)std::min<long long>(chunk, B - c0);
+            rc = refgrad_run(*fp, *bp, m, fv.data() + c0 * Pf, bv.data() + c0 * Pb, x0.data() + c0 * nf,
+                             a0.data() + c0 * na, exc.data() + c0, *signals_, h_, (int)numsteps_, (int)save,
+                             o.data() + c0 * na, stream_, err);
+            if (rc) return rc;
+        }
         for (int b = 0; b < B; ++b) {
             const int e = b / nb, c = b % nb;
             const Block& bl = blocks[ids[c]];

@@ -41,11 +41,23 @@ struct Block {
 };
 
 // Blocks sharing one pattern, solved as one batch (instances = blocks x signals).
+// The instances' inputs stay on the host too: a sweep larger than the device
+// memory budget runs as sequential batches of `chunk` instances.
 struct Group {
     std::vector<int> blocks;
     std::shared_ptr<Plan> plan, aplan;
     std::unique_ptr<Batch> batch;
+    std::vector<double> hvals, hx0;   // [B][P], [B][n]; instance b = signal b / nb, block b % nb
+    std::vector<int> hexc;            // [B]
+    int resident = 0;                 // instances whose inputs the batch holds from instance 0 (0: none)
 };
+
+// Instances per sequential batch of a sweep of n_instances that need
+// bytes_per_instance of device memory each, within `budget` bytes: all of
+// them when they fit, else as many as fit; 0 when not even one does.  The
+// reference splits its excitation copies the same way by free memory
+// (numberOfSimulationToPerform, src/__GpuDriver.cu:420-449, 896-938).
+long long sweep_chunk(long long n_instances, long long bytes_per_instance, long long budget);
 
 class Driver {
 public:
@@ -67,6 +79,13 @@ public:
     int trajectory(unsigned save, std::vector<double>* out, std::string* err);
     int gradient(unsigned save, std::vector<double>* out, std::string* err);
     int last_kind() const { return last_kind_; }
+    // Device memory a solve may use for its instances (0: automatic, 90 % of
+    // what is free when the solve starts plus what the driver holds); a sweep
+    // beyond it runs as sequential batches.  No reference counterpart as an
+    // argument: the reference always takes the free memory.
+    int set_memory_budget(long long bytes, std::string* err);
+    // Sequential batches the last solve ran (1: the whole sweep at once).
+    int last_chunks() const { return last_chunks_; }
     // Output sizes of the getters (no solve): nf * n_exc, na * n_exc and
     // floor(nf * n_exc * numsteps / save) (src/__GpuDriver.cu:420,469,580).
     long long amplitudes_size() const { return (long long)nf_ * n_exc_; }
@@ -101,7 +120,10 @@ private:
     std::vector<Group> groups_;
     std::shared_ptr<Signals> signals_;
     int last_kind_ = kNone;
+    long long mem_budget_ = 0;
+    int last_chunks_ = 0;
     cudaStream_t stream_ = nullptr;
+    long long budget_for(long long held) const;
 };
 
 }  // namespace pasif

@@ -426,6 +426,7 @@ bool Batch::fwd_kernel(const Signals& sig, unsigned long long mm, unsigned long 
     key.wn.assign(sig.im_host.begin(), sig.im_host.begin() + sig.w);
     key.wc.assign(sig.im_host.begin() + sig.w, sig.im_host.end());
     key.slices = plan->slicing < 0 ? 0 : ws_slices(pat, f, plan->slicing > 0, B, ext());
+    key.fast = plan->fast && traj_mode == 0 && !ext() && key.slices < 2;
     return get_fwd_kernel(pat, lit, key, k, jerr);
 }
 

@@ -83,6 +83,7 @@ struct Plan {
     bool generic_only = false;
     bool no_literals = false;   // every value loaded: one kernel for all batches
     int slicing = 0;            // warp-sliced kernels: 0 by size, 1 always, -1 never
+    bool fast = false;          // PASIF_PLAN_FAST: fast thread-per-system forward kernels (not the oracle's bits)
     DevBuf gpat;           // flat pattern for the generic kernels (uploaded on first use)
     pk::GenPattern gen() const;
     int ensure_device(std::string* err);

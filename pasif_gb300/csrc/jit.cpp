@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -67,6 +68,89 @@ struct Emitter {
         if (slot_lo[q] >= 0) return "q[" + std::to_string(slot_lo[q]) + "]";
         if (lit.value_lo[q] == 0.0) return "";
         return hexlit(lit.value_lo[q]);
+    }
+
+    // rhs body of the fast kernels (PASIF_PLAN_FAST): the products of state
+    // components are formed once per evaluation and shared by every term that
+    // uses them (operands sorted, built from the shared prefix), values 1 and
+    // -1 fold into an add / subtract, each destination sums its terms in one
+    // fma chain (two, added at the end, from four terms on), and the chains of
+    // all destinations are emitted interleaved.  Not the canonical order: the
+    // results differ from the oracle's in the last bits.
+    void rhs_fast(std::ostringstream& o, bool force) const {
+        const int n = pat.n;
+        const int go = pat.k_nnz(), lo = go + pat.g_nnz(), po = lo + pat.l_nnz(), fo = po + pat.p_nnz();
+        auto S = [](int v) { return std::to_string(v); };
+        struct T { int q; std::vector<int> ops; bool force; };
+        std::vector<std::vector<T>> terms(n);
+        for (int i = 0; i < n; ++i)
+            for (int q = pat.k_ptr[i]; q < pat.k_ptr[i + 1]; ++q) terms[i].push_back({q, {pat.k_col[q]}, false});
+        for (int e = 0; e < pat.g_nnz(); ++e) {
+            const int* ix = &pat.g_idx[3 * e];
+            terms[ix[0]].push_back({go + e, {ix[1], ix[2]}, false});
+        }
+        for (int e = 0; e < pat.l_nnz(); ++e) {
+            const int* ix = &pat.l_idx[4 * e];
+            terms[ix[0]].push_back({lo + e, {ix[1], ix[2], ix[3]}, false});
+        }
+        for (int e = 0; e < pat.p_nnz(); ++e) {
+            const int* ix = &pat.p_idx[5 * e];
+            terms[ix[0]].push_back({po + e, {ix[1], ix[2], ix[3], ix[4]}, false});
+        }
+        if (force)
+            for (int e = 0; e < pat.f_nnz(); ++e) terms[pat.f_idx[e]].push_back({fo + e, {}, true});
+        std::map<std::vector<int>, std::string> mono;
+        int nm = 0;
+        std::function<std::string(const std::vector<int>&)> get = [&](const std::vector<int>& ops) -> std::string {
+            if (ops.size() == 1) return "xs[" + S(ops[0]) + "]";
+            auto it = mono.find(ops);
+            if (it != mono.end()) return it->second;
+            const std::string a = get(std::vector<int>(ops.begin(), ops.end() - 1));
+            const std::string name = "mo" + S(nm++);
+            o << "      const R " << name << " = m::mul(" << a << ", xs[" << S(ops.back()) << "]);\n";
+            mono[ops] = name;
+            return name;
+        };
+        // chains: (destination, chain index) -> the terms' (coefficient, monomial)
+        struct Ch { int i, c; std::vector<std::pair<std::string, std::string>> t; };
+        std::vector<Ch> chains;
+        std::vector<int> nch(n, 0);
+        for (int i = 0; i < n; ++i) {
+            nch[i] = terms[i].size() >= 4 ? 2 : (terms[i].empty() ? 0 : 1);
+            for (int c = 0; c < nch[i]; ++c) chains.push_back({i, c, {}});
+        }
+        for (int i = 0, base = 0; i < n; base += nch[i], ++i)
+            for (size_t k = 0; k < terms[i].size(); ++k) {
+                std::vector<int> ops = terms[i][k].ops;
+                std::sort(ops.begin(), ops.end());
+                const std::string m = terms[i][k].force ? "u" : get(ops);
+                chains[base + (int)(k % (size_t)nch[i])].t.push_back({val(terms[i][k].q), m});
+            }
+        auto lit_is = [](const std::string& c, double v) { return c == hexlit(v); };
+        size_t longest = 0;
+        for (const Ch& c : chains) longest = std::max(longest, c.t.size());
+        for (const Ch& c : chains) o << "      R c" << c.i << "_" << c.c << ";\n";
+        for (size_t k = 0; k < longest; ++k)
+            for (const Ch& c : chains) {
+                if (k >= c.t.size()) continue;
+                const std::string acc = "c" + S(c.i) + "_" + S(c.c);
+                const std::string& co = c.t[k].first;
+                const std::string& mo = c.t[k].second;
+                if (k == 0) {
+                    if (lit_is(co, 1.0)) o << "      " << acc << " = " << mo << ";\n";
+                    else if (lit_is(co, -1.0)) o << "      " << acc << " = -" << mo << ";\n";
+                    else o << "      " << acc << " = m::mul(" << co << ", " << mo << ");\n";
+                } else {
+                    if (lit_is(co, 1.0)) o << "      " << acc << " = m::add(" << acc << ", " << mo << ");\n";
+                    else if (lit_is(co, -1.0)) o << "      " << acc << " = m::sub(" << acc << ", " << mo << ");\n";
+                    else o << "      " << acc << " = m::fma(" << co << ", " << mo << ", " << acc << ");\n";
+                }
+            }
+        for (int i = 0; i < n; ++i) {
+            if (nch[i] == 0) o << "      f[" << i << "] = R(0);\n";
+            else if (nch[i] == 1) o << "      f[" << i << "] = c" << i << "_0;\n";
+            else o << "      f[" << i << "] = m::add(c" << i << "_0, c" << i << "_1);\n";
+        }
     }
 
     // rhs_lo body: f = the right-hand side of the low parts of the values, one
@@ -753,7 +837,7 @@ static void emit_sample_ring(std::ostringstream& o, int W, int block, const Patt
 }
 
 namespace {
-void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32);
+void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32, bool fast = false);
 }
 
 std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key) {
@@ -762,12 +846,13 @@ std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelK
     const int n = pat.n;
     std::ostringstream o;
     o << "// generated by pasif_gb300 jit.cpp: forward RK4, n=" << n << " P=" << pat.P()
-      << (key.ext ? " extended state" : "") << "\n";
-    emit_sys_head(o, pat, em, key.f32);
+      << (key.ext ? " extended state" : "") << (key.fast ? " fast" : "") << "\n";
+    emit_sys_head(o, pat, em, key.f32, key.fast);
     o << "};\n";
     // forcing window and weights as compile-time constants
     const int W = key.window;
     o << "struct JW {\n  static constexpr int W = " << W << ";\n";
+    o << "  static constexpr bool FAST = " << (key.fast ? "true" : "false") << ";\n";
     emit_sample_ring(o, W, key.block, pat);
     for (int which = 0; which < 2; ++which) {
         o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";
@@ -799,7 +884,7 @@ bool fwd_compile_report(const Pattern& pat, const Literals& lit, const FwdKernel
 namespace {
 
 // JSys members shared by the forward and adjoint programs: values, load, rhs.
-void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32) {
+void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32, bool fast) {
     o << "#include \"rk4_core.cuh\"\n";
     o << "namespace pk {\n";
     o << "typedef " << (f32 ? "float" : "double") << " R;\n";
@@ -823,6 +908,16 @@ void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em,
     }
     o << "  template <bool FORCE, class V, class W, class F>\n";
     o << "  __device__ __forceinline__ void rhs(const V& xs, const W& xp, R u, F& f) const {\n";
+    if (fast) {   // forward systems only: xs and xp are the same vector
+        o << "    typedef M<R> m;\n    (void)xp;\n";
+        o << "    if (FORCE) {\n";
+        em.rhs_fast(o, true);
+        o << "    } else {\n";
+        em.rhs_fast(o, false);
+        o << "    }\n";
+        o << "  }\n";
+        return;
+    }
     o << "    typedef M<R> m;\n    R a, c;\n";
     o << "    if (FORCE) {\n";
     em.rhs(o, true);
@@ -1042,6 +1137,7 @@ std::string pool_source(const Pattern& pat, const FwdKernelKey& key) {
     o << "};\n";
     const int W = key.window;
     o << "struct JW {\n  static constexpr int W = " << W << ";\n";
+    o << "  static constexpr bool FAST = false;\n";
     emit_sample_ring(o, W, key.block, pat);
     for (int which = 0; which < 2; ++which) {
         o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";

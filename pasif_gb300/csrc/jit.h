@@ -33,6 +33,7 @@ struct FwdKernelKey {
     std::vector<double> wn, wc;     // its weights in the compute precision
     int slices = 0;                 // >= 2: warp-sliced kernel with that many warps per 32 systems
     bool ext = false;               // extended-state mode (FP32 stages, double-float state, low parts of the values)
+    bool fast = false;              // PASIF_PLAN_FAST: shared products, folded RK sum (not the oracle's bits)
 };
 
 struct JitKernel {

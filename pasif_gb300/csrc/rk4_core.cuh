@@ -297,13 +297,42 @@ struct GenSys {
 // the parameters; the step adds, beside h/6 (k1 + 2k2 + 2k3 + k4), the term
 // h f_lo(Q) of the low parts of the FP64 parameters (JSys::rhs_lo), evaluated
 // once at the start of the step, with ext_update (h6lo: low part of h/6).
-template <typename R, int N, bool KAHAN, int NSTG = 0, bool EXT = false, class Sys, class V>
+// FAST (fast kernels, PASIF_PLAN_FAST): the step's increment is summed as
+// h/6 k1 - c + h/3 k2 + h/3 k3 + h/6 k4 directly (the compensation folded into
+// its first fma, h/3 = 2 h6 exactly) instead of h/6 ((k1 + 2k2) + 2k3 + k4) - c:
+// the same compensated update in fewer operations, not the oracle's bits.
+template <typename R, int N, bool KAHAN, int NSTG = 0, bool EXT = false, bool FAST = false, class Sys, class V>
 __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K, V& Mi,
                                          R ua, R ub, R uc, R h, R h2, R h6, R* stg = nullptr, long long sB = 0,
                                          R h6lo = R(0)) {
     typedef M<R> m;
     static_assert(!EXT || N > 0, "extended-state steps need a compile-time state size");
+    static_assert(!FAST || (!EXT && NSTG == 0), "fast steps are plain forward steps");
     const int n = N ? N : sys.dim();
+    if constexpr (FAST) {
+        const R h3 = m::add(h6, h6);
+        sys.template rhs<true>(Q, Q, ua, K);
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            S[i] = m::fma(h6, K[i], KAHAN ? -Cm[i] : R(0));
+            Mi[i] = m::fma(h2, K[i], Q[i]);
+        }
+        sys.template rhs<true>(Mi, Mi, ub, K);
+#pragma unroll
+        for (int i = 0; i < n; ++i) { S[i] = m::fma(h3, K[i], S[i]); Mi[i] = m::fma(h2, K[i], Q[i]); }
+        sys.template rhs<true>(Mi, Mi, ub, K);
+#pragma unroll
+        for (int i = 0; i < n; ++i) { S[i] = m::fma(h3, K[i], S[i]); Mi[i] = m::fma(h, K[i], Q[i]); }
+        sys.template rhs<true>(Mi, Mi, uc, K);
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const R y = m::fma(h6, K[i], S[i]);
+            const R t = m::add(Q[i], y);
+            if (KAHAN) Cm[i] = m::sub(m::sub(t, Q[i]), y);
+            Q[i] = t;
+        }
+        return;
+    }
     if constexpr (NSTG >= 1) {
 #pragma unroll
         for (int i = 0; i < n; ++i) stg[i * sB] = Q[i];
@@ -478,6 +507,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
                                             R& sq, R& sqc) {
     typedef M<R> m;
     constexpr int W = WP::W;
+    constexpr bool FASTK = WP::FAST && HTRAJ == 0 && !EXT;   // fast steps: plain forwards only
     constexpr unsigned SPI = W == 0 ? 1u : (unsigned)(W / 2);
     constexpr int STG = HTRAJ == 2 ? adj_slot_vecs<R>() : 0;
     const long long B = a.B;
@@ -533,9 +563,9 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     const unsigned end = rc.step0 + rc.nsteps;
     while (s < end && (s % SPI) != 0u) {
         pre(s);
-        rk4_step<R, N, KAHAN, STG, EXT>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
-                                        force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2,
-                                        a.h6, slot(s), B, a.h6lo);
+        rk4_step<R, N, KAHAN, STG, EXT, FASTK>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
+                                               force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h,
+                                               a.h2, a.h6, slot(s), B, a.h6lo);
         post(s);
         ++s;
     }
@@ -582,8 +612,8 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
                     else un = g1 ? m::fma(WP::wc(0), x1, m::mul(WP::wn(0), x2)) : R(0);
                 }
                 pre(s + (unsigned)r);
-                rk4_step<R, N, KAHAN, STG, EXT>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6,
-                                                slot(s + (unsigned)r), B, a.h6lo);
+                rk4_step<R, N, KAHAN, STG, EXT, FASTK>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6,
+                                                       slot(s + (unsigned)r), B, a.h6lo);
                 post(s + (unsigned)r);
                 uc = un;
             }
@@ -595,9 +625,9 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     }
     while (s < end) {
         pre(s);
-        rk4_step<R, N, KAHAN, STG, EXT>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
-                                        force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h, a.h2,
-                                        a.h6, slot(s), B, a.h6lo);
+        rk4_step<R, N, KAHAN, STG, EXT, FASTK>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
+                                               force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h,
+                                               a.h2, a.h6, slot(s), B, a.h6lo);
         post(s);
         ++s;
     }

@@ -86,3 +86,23 @@ def test_plan_without_device_and_bad_precision():
     Plan(pat, "fp64")
     with pytest.raises(N.PasifError):
         Plan(pat, 7)
+
+
+def test_sweep_chunk_rule():
+    """Memory-bounded sweeps: all instances at once when they fit the budget,
+    else as many per sequential batch as fit, none when one does not."""
+    import ctypes as C
+    from pasif_gb300 import _native as N
+    out = C.c_longlong()
+
+    def chunk(n, per, budget):
+        N.check(N.lib.pasif_sweep_chunk(n, per, budget, C.byref(out)))
+        return out.value
+
+    assert chunk(1000, 100, 10 ** 6) == 1000
+    assert chunk(1000, 100, 10_000) == 100
+    assert chunk(1000, 100, 10_050) == 100
+    assert chunk(1000, 100, 99) == 0
+    assert chunk(0, 100, 10) == 0
+    assert chunk(7, 0, 0) == 7
+    assert N.lib.pasif_sweep_chunk(-1, 1, 1, C.byref(out)) == N.ERR_INVALID

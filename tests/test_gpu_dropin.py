@@ -201,3 +201,98 @@ def test_error_behaviour(gpu):
         p._getAmplitudes()
     with pytest.raises(ValueError):
         p._setInterpolationMatrix(np.ones(12), 6)
+
+
+class _Rec:
+    """A concatenated system as recorded from the setter arguments."""
+
+    def __init__(self, calls, fwd=True):
+        tag = "Fwd" if fwd else "Bwd"
+        d = {m: a for m, a in calls}
+        shape, data, ind, ptr = d[f"_set{tag}K"]
+        self.K = csr_like(data, ind, ptr, shape)
+        self.gam = tens(*d[f"_set{tag}Gamma"])
+        self.lam = tens(*d[f"_set{tag}Lambda"])
+        self.psi = tens(*d[f"_set{tag}Psi"])
+        self.force = np.asarray(d[f"_set{tag}ForcePattern"][0], float)
+        self.ic = np.asarray(d[f"_set{tag}InitialConditions"][0], float)
+
+
+def csr_like(data, ind, ptr, shape):
+    from scipy.sparse import csr_matrix
+    return csr_matrix((np.asarray(data, float), np.asarray(ind), np.asarray(ptr)), shape=tuple(int(s) for s in shape))
+
+
+def tens(dims, val, idx):
+    t = coo_tensor([int(x) for x in dims])
+    t.val = [float(x) for x in np.asarray(val).reshape(-1)]
+    t.indices = [int(x) for x in np.asarray(idx).reshape(-1)]
+    return t
+
+
+@pytest.mark.parametrize("case", ["coupled2x6", "probe1", "jacobian2", "interp"])
+def test_reference_front_end_calls_replayed_on_the_drop_in(gpu, case):
+    """The driver calls the reference's own PASIf.py makes (recorded in
+    tests/golden/frontend_calls_<case>.npz) replayed on the drop-in __GpuDriver:
+    _getAmplitudes (and _getGradient with a jacobian) equal the oracle's
+    restatement on the recorded concatenated system, bit for bit."""
+    from pasif_gb300 import PASIfgpu
+    from tests.test_frontend_ref import load_calls
+    calls = load_calls(case)
+    init = calls[0][1]
+    exc = np.asarray(init[0], float)
+    sr, N = int(init[1]), int(init[2])
+    drv = getattr(PASIfgpu, "__GpuDriver")(list(exc), sr, N, bool(init[3]), bool(init[4]), bool(init[5]), int(init[6]))
+    window, im = 0, None
+    for meth, args in calls[1:]:
+        if meth == "_setInterpolationMatrix":
+            window, im = int(args[1]), np.asarray(args[0], float)
+        getattr(drv, meth)(*args)
+    f = _Rec(calls)
+    fpat, fvals = oracle_system(f.K, f.gam, f.lam, f.force)
+    imr = im[:2 * window].reshape(2, window) if window else None
+    got = np.asarray(drv._getAmplitudes())
+    ref = O.get_amplitudes(fpat, fvals, f.ic, exc, 1 / sr, N, window, imr)
+    np.testing.assert_array_equal(got, ref)
+    if any(m == "_setBwdK" for m, _ in calls):
+        b = _Rec(calls, fwd=False)
+        bpat, bvals = oracle_system(b.K, b.gam, b.lam, b.force, b.psi, n_sp=fpat.n)
+        got = np.asarray(drv._getGradient(0))
+        ref = O.get_gradient(fpat, fvals, f.ic, bpat, bvals, b.ic, exc, 1 / sr, N)
+        np.testing.assert_array_equal(got, ref)
+
+
+def test_memory_bounded_sweep_equals_one_batch(gpu):
+    """A sweep run as sequential batches (small device-memory budget) equals
+    the one-batch solve bit for bit: amplitudes, trajectory and gradient, every
+    instance on its own signal (the reference's chunks read the wrong
+    excitation offset, src/__GpuDriver.cu:912-924).  A budget below one
+    instance is refused with a memory error."""
+    rng = np.random.default_rng(41)
+    E, L, N = 7, 160, 120
+    exc = [np.sin(0.03 * (e + 1) * np.arange(L)) + 0.1 * rng.standard_normal(L) for e in range(E)]
+
+    def make(budget, grad=False):
+        p = PASIf(exc, 32, N)
+        if grad:
+            p.setSystems(*[list(z) for z in zip(*[probe_system(), probe_system(), probe_system()])])
+            p.setJacobian(*[list(z) for z in zip(*[adjoint_inputs(), adjoint_inputs(), adjoint_inputs()])])
+        else:
+            p.setSystems(*[list(z) for z in zip(*[probe_system(), random_user_system(np.random.default_rng(42), 3),
+                                                  probe_system()])])
+        if budget:
+            p._setMemoryBudget(budget)
+        return p
+
+    whole, split = make(0), make(2000)
+    a0, a1 = np.asarray(whole.getAmplitudes()), np.asarray(split.getAmplitudes())
+    assert split._lastChunks() > whole._lastChunks() >= 1
+    np.testing.assert_array_equal(a0, a1)
+    np.testing.assert_array_equal(np.asarray(whole._getTrajectory(7)), np.asarray(split._getTrajectory(7)))
+    assert split._lastChunks() > whole._lastChunks()
+    whole, split = make(0, True), make(3000, True)
+    np.testing.assert_array_equal(np.asarray(whole.getGradient()), np.asarray(split.getGradient()))
+    assert split._lastChunks() > whole._lastChunks()
+    tiny = make(1)
+    with pytest.raises(RuntimeError, match="memory"):
+        tiny.getAmplitudes()

@@ -215,6 +215,7 @@ int Batch::reserve(int n_sys, int nsteps, std::string* err) {
     const size_t full_bytes = Bn * n * (slot_vecs() * (size_t)nsteps + 1) * rs;
     PK_CUDA(buf.ensure(std::max(chunk_bytes, nsteps > 0 ? std::min(full_bytes, adj_store_limit) : 0)), "cudaMalloc");
     PK_CUDA(pbar.ensure(Bn * P * sizeof(double)), "cudaMalloc");
+    if (f32()) PK_CUDA(pkbuf.ensure(Bn * 2 * P * sizeof(float)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(gfin.ensure(Bn * n * rs), "cudaMalloc");
     PK_CUDA(gsq.ensure(Bn * rs), "cudaMalloc");
@@ -609,6 +610,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     }
     if (replayed) PK_CUDA(adj_state.ensure(vec), "cudaMalloc");
     PK_CUDA(pbar.ensure(Bn * (size_t)(P > 0 ? P : 1) * sizeof(double)), "cudaMalloc");
+    if (f) PK_CUDA(pkbuf.ensure(Bn * 2 * (size_t)(P > 0 ? P : 1) * sizeof(float)), "cudaMalloc");
     PK_CUDA(dx0.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     if (g_final) {
         int rc = upload_interleaved(g_final, B, n, f, memory, gfin, adj_stage, st, err);
@@ -656,7 +658,8 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     a.h6lo = (R_)(h / 6.0 - (double)(R_)(h / 6.0));                   \
     a.sq_start = red.sq_start;                                        \
     a.sq_mask = g_sq ? sm : 0ull;                                     \
-    a.stored = stored || replayed ? 1 : 0;
+    a.stored = stored || replayed ? 1 : 0;                             \
+    a.pk = f ? pkbuf.as<R_>() : nullptr;
     const dim3 grid((unsigned)(jit ? (B + jk.per_block - 1) / jk.per_block : (B + 127) / 128));
     if (jit && compensated()) PK_CUDA(lamc.ensure(Bn * (size_t)n * rs), "cudaMalloc");
     // Specialised kernels over many blocks: forward segments and backward chunk

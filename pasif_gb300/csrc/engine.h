@@ -111,6 +111,7 @@ struct Batch {
     DevBuf vals, x0, state, exc, out_max, out_sq, scratch, stage, traj;
     DevBuf ckpt, buf, pbar, dx0, gfin, gsq, adj_stage, lamc, adj_state;
     DevBuf split;                 // kFP32Ext: values / x0 split into high and low parts (device inputs)
+    DevBuf pkbuf;                 // FP32 adjoints: [2P][B] compensated per-chunk gradient totals
     Literals lit;
     int n_max = 0;
     bool has_sq = false;

@@ -764,12 +764,26 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             o << "  __device__ __forceinline__ void zero_pbar(double* pbar, long long B, int b) const {\n";
             for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = 0.0;\n";
             o << "  }\n";
-            o << "  template <bool SC, class PV> __device__ __forceinline__ void add_pbar(const PV& ps, double* pbar,"
-                 " long long B, int b, double s) const {\n";
+            // FP32 compensated per-chunk totals in global memory (sum at q, compensation at P + q)
+            const int Pt = pat.P();
+            o << "  template <class PV> __device__ __forceinline__ void add_pk(const PV& ps, R* pk, long long B, int b)"
+                 " const {\n";
             for (auto& kv : pslot)
-                o << "    pbar[" << kv.first << "LL * B + b] = SC ? M<double>::fma(s, (double)ps[" << kv.second
-                  << "], pbar[" << kv.first << "LL * B + b]) : pbar[" << kv.first << "LL * B + b] + (double)ps["
-                  << kv.second << "];\n";
+                o << "    { R s_ = pk[" << kv.first << "LL * B + b], c_ = pk[" << (Pt + kv.first)
+                  << "LL * B + b]; kahan_add(s_, c_, ps[" << kv.second << "]); pk[" << kv.first
+                  << "LL * B + b] = s_; pk[" << (Pt + kv.first) << "LL * B + b] = c_; }\n";
+            o << "  }\n";
+            o << "  template <bool EXT> __device__ __forceinline__ void flush_pk(R* pk, double* pbar, long long B,"
+                 " int b, double s) const {\n";
+            for (auto& kv : pslot)
+                o << "    { const double t_ = (double)pk[" << kv.first << "LL * B + b] - (double)pk["
+                  << (Pt + kv.first) << "LL * B + b]; pbar[" << kv.first << "LL * B + b] = EXT ? M<double>::fma(s, t_, "
+                  << "pbar[" << kv.first << "LL * B + b]) : pbar[" << kv.first << "LL * B + b] + t_; pk["
+                  << kv.first << "LL * B + b] = R(0); pk[" << (Pt + kv.first) << "LL * B + b] = R(0); }\n";
+            o << "  }\n";
+            o << "  __device__ __forceinline__ void zero_pk(R* pk, long long B, int b) const {\n";
+            for (auto& kv : pslot)
+                o << "    pk[" << kv.first << "LL * B + b] = R(0); pk[" << (Pt + kv.first) << "LL * B + b] = R(0);\n";
             o << "  }\n";
         }
         o << "};\n";

@@ -135,6 +135,10 @@ struct AdjArgs {
     // per step without the h/6 factor and added as (h6 + h6lo) * sum in FP64.
     int ext;
     R h6lo;
+    // FP32 adjoints: [2P][B] compensated FP32 totals of the chunk's gradient
+    // sums (sum, compensation) for the values whose totals do not stay in
+    // registers; flushed into pbar (FP64) at the end of every chunk
+    R* pk;
 };
 
 // __GpuDriver::_getGradient semantics (see the oracle for the quirk list).

@@ -782,8 +782,12 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
     // launch (the same additions as into pbar, in the same order)
     constexpr bool PBREG = STEP_ACC && P <= 24;
     RegVec<double, PBREG ? P : 1> PR;
+    // per-step sums added with compensation to FP32 totals, flushed into the
+    // FP64 totals once per chunk of C steps (FP64 adds run at 1/64 of the FP32
+    // rate on GB300: once per step they were a large part of the step)
+    RegVec<R, PBREG ? P : 1> PK, PKC;
 #pragma unroll
-    for (int p = 0; p < (PBREG ? P : 1); ++p) PR[p] = 0.0;
+    for (int p = 0; p < (PBREG ? P : 1); ++p) { PR[p] = 0.0; PK[p] = R(0); PKC[p] = R(0); }
     if (khi == a.nck - 1) {
         if (a.stored && !PBREG)   // no forward pass in this kernel zeroed the totals
             for (int p = 0; p < P; ++p) PB[p] = 0.0;
@@ -803,6 +807,9 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
         const int slot0 = a.stored ? a.slot_base : start;   // buf slot of step t: t - slot0
+        if constexpr (STEP_ACC && !PBREG) {
+            for (int p = 0; p < 2 * P; ++p) a.pk[(long long)p * B + b] = R(0);
+        }
         if (!a.stored) {
             const R* ck = a.ckpt + (long long)k * 2 * N * B + b;
 #pragma unroll
@@ -938,18 +945,37 @@ __device__ __forceinline__ void adj_run_jit(const Sys& sys, const AdjArgs<R>& a,
                 else LAM[i] = m::add(QB[i], YB[i]);
                 QN[i] = QC[i];
             }
-            if constexpr (PBREG) {
+            if constexpr (PBREG) {   // compensated FP32 sums of this chunk (see PK)
 #pragma unroll
                 for (int p = 0; p < P; ++p) {
-                    PR[p] = EXT ? M<double>::fma(h6d, (double)pacc[p], PR[p]) : PR[p] + (double)pacc[p];
+                    kahan_add(PK[p], PKC[p], pacc[p]);
                     pacc[p] = R(0);
                 }
-            } else if (STEP_ACC) {
-#pragma unroll
+            } else if (STEP_ACC) {   // the same compensated sums, in a.pk
                 for (int p = 0; p < P; ++p) {
-                    PB[p] = EXT ? M<double>::fma(h6d, (double)pacc[p], PB[p]) : PB[p] + (double)pacc[p];
+                    R sm = a.pk[(long long)p * B + b], cm = a.pk[(long long)(P + p) * B + b];
+                    kahan_add(sm, cm, pacc[p]);
+                    a.pk[(long long)p * B + b] = sm;
+                    a.pk[(long long)(P + p) * B + b] = cm;
                     pacc[p] = R(0);
                 }
+            }
+        }
+        if constexpr (STEP_ACC && !PBREG) {
+            for (int p = 0; p < P; ++p) {
+                const double sum = (double)a.pk[(long long)p * B + b] - (double)a.pk[(long long)(P + p) * B + b];
+                PB[p] = EXT ? M<double>::fma(h6d, sum, PB[p]) : PB[p] + sum;
+                a.pk[(long long)p * B + b] = R(0);
+                a.pk[(long long)(P + p) * B + b] = R(0);
+            }
+        }
+        if constexpr (PBREG) {   // the chunk's compensated FP32 sums into the FP64 totals
+#pragma unroll
+            for (int p = 0; p < P; ++p) {
+                const double sum = (double)PK[p] - (double)PKC[p];
+                PR[p] = EXT ? M<double>::fma(h6d, sum, PR[p]) : PR[p] + sum;
+                PK[p] = R(0);
+                PKC[p] = R(0);
             }
         }
     }
@@ -1420,8 +1446,15 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     constexpr bool PBREG = !STEP_ACC || PO <= 16;
     RegVec<double, PBREG ? PO : 1> PB;
     RegVec<R, STEP_ACC ? PO : 1> pst;
+    // FP32 with the totals in registers: the per-step sums go with
+    // compensation into FP32 totals (PK, PKC), flushed into the FP64 totals
+    // once per chunk (FP64 adds run at 1/64 of the FP32 rate on GB300)
+    constexpr bool PKREG = STEP_ACC && PBREG;
+    RegVec<R, PKREG ? PO : 1> PK, PKC;
 #pragma unroll
     for (int p = 0; p < (PBREG ? PO : 1); ++p) PB[p] = 0.0;
+#pragma unroll
+    for (int p = 0; p < (PKREG ? PO : 1); ++p) { PK[p] = R(0); PKC[p] = R(0); }
 #pragma unroll
     for (int p = 0; p < (STEP_ACC ? PO : 1); ++p) pst[p] = R(0);
     V Q, Cm, S, K, Mi;
@@ -1494,6 +1527,9 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
         const int slot0 = a.stored ? a.slot_base : start;   // buf slot of step t: t - slot0
+        if constexpr (STEP_ACC && !PKREG) {
+            if (valid) sl.zero_pk(a.pk, B, b);
+        }
         if (!a.stored) {
             const R* ck = a.ckpt + (long long)k * 2 * N * B;
             sl.load_vec(Q, ck, B, b);
@@ -1643,15 +1679,25 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
             if constexpr (STEP_ACC) {
                 if constexpr (PBREG) {
 #pragma unroll
-                    for (int p = 0; p < PO; ++p)
-                        PB[p] = EXT ? M<double>::fma(h6d, (double)pst[p], PB[p]) : PB[p] + (double)pst[p];
-                } else {
-                    if (valid) sl.template add_pbar<EXT>(pst, a.pbar, B, b, h6d);
+                    for (int p = 0; p < PO; ++p) kahan_add(PK[p], PKC[p], pst[p]);
+                } else {   // the same compensated sums, in a.pk
+                    if (valid) sl.add_pk(pst, a.pk, B, b);
                 }
 #pragma unroll
                 for (int p = 0; p < PO; ++p) pst[p] = R(0);
             }
             pk_block_sync();   // every slice is done with this step's regions
+        }
+        if constexpr (PKREG) {   // the chunk's compensated FP32 sums into the FP64 totals
+#pragma unroll
+            for (int p = 0; p < PO; ++p) {
+                const double sum = (double)PK[p] - (double)PKC[p];
+                PB[p] = EXT ? M<double>::fma(h6d, sum, PB[p]) : PB[p] + sum;
+                PK[p] = R(0);
+                PKC[p] = R(0);
+            }
+        } else if constexpr (STEP_ACC) {
+            if (valid) sl.template flush_pk<EXT>(a.pk, a.pbar, B, b, h6d);
         }
     }
     if (!valid) return;

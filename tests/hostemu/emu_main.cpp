@@ -290,6 +290,8 @@ int main(int argc, char** argv) {
     a.sq_start = sq_start;
     std::vector<R> lamc((size_t)B * n, R(0));
     a.lamc = lamc.data();
+    std::vector<R> pk((size_t)B * 2 * (P > 0 ? P : 1), R(0));
+    a.pk = pk.data();
     // EMU_ADJ_STORED=1: backward over a stored trajectory ([nsteps+1][4][n][B]
     // slots).  It is made by this kernel's own chunk recompute: the adjoint of
     // one step more, in one chunk, leaves slots 0..nsteps in its buffer.

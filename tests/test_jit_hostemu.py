@@ -336,3 +336,23 @@ def test_generated_adjoint_split_launches(tmp_path, prec, slicing, split):
         out.append(run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, N // 3, split=sp))
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("prec", ["fp32_kahan", "fp32_ext"])
+def test_generated_adjoint_chain16_sliced_equals_thread(tmp_path, prec):
+    """A 32-state chain (87 values): the gradient totals of both layouts do not
+    fit registers and go through the compensated FP32 totals in memory; the
+    warp-sliced and thread-per-system adjoints still agree bit for bit."""
+    w = synth.chain8(n_sys=5, nsteps=45, nd=16)
+    rng = np.random.default_rng(37)
+    gf = rng.normal(size=(w.n_sys, w.pattern.n))
+    gs = rng.normal(size=w.n_sys)
+    out = []
+    for slicing in (False, True):
+        d = os.path.join(str(tmp_path), str(slicing))
+        os.makedirs(d)
+        out.append(run_emulated_adjoint(d, w.pattern, prec, slicing, w.values, w.x0, w.exc_index, w.signals,
+                                        np.asarray(w.im), gf, gs, w.nsteps, (0, 3), 20, h=w.h))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert np.abs(out[0][0]).max() > 0

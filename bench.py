@@ -317,6 +317,12 @@ def main():
     relx = np.abs(rmsx - rms64) / np.abs(rms64)
     del bx
 
+    import ctypes
+    peak = ctypes.c_double()
+    N.check(N.lib.pasif_fma_peak(N.FP32, ctypes.byref(peak)))
+    peak64 = ctypes.c_double()
+    N.check(N.lib.pasif_fma_peak(N.FP64, ctypes.byref(peak64)))
+
     # adjoint gradients/s: 8-DOF chain, 4096 systems x 50000 steps, gradients of
     # the final-half sum of squared positions w.r.t. every value (FP32 + FP64 check)
     from pasif_gb300 import synth
@@ -338,9 +344,16 @@ def main():
         dt = time.perf_counter() - t0
         key = prec if storage == 0 else prec + "_stored_trajectory"
         grads[key] = dv
+        adj_fl = c3.pattern.adjoint_flops_per_step(len(c3.sq_comp))
+        pk = peak64.value if prec == "fp64" else peak.value
         adj[key] = {"gradients_per_s": c3.n_sys / dt, "adjoint_system_steps_per_s": c3.n_sys * c3.nsteps / dt,
                     "seconds": dt, "kernel": bt.kernel_info()["adjoint"],
-                    "trajectory": "sqrt(N) checkpoints" if storage == 0 else "stored (one forward pass)"}
+                    "trajectory": "sqrt(N) checkpoints" if storage == 0 else "stored (one forward pass)",
+                    "roofline": {"bound": "fp64_fma" if prec == "fp64" else "fp32_fma",
+                                 "flops_per_adjoint_system_step": adj_fl,
+                                 "achieved_tflops": adj_fl * c3.n_sys * c3.nsteps / dt / 1e12,
+                                 "frac": adj_fl * c3.n_sys * c3.nsteps / dt / pk,
+                                 "note": "wall time of the C-ABI call, every launch and copy included"}}
         del bt
     adj["fp32_kahan_stored_trajectory"]["equals_checkpointed"] = bool(
         np.array_equal(grads["fp32_kahan"], grads["fp32_kahan_stored_trajectory"]))
@@ -437,15 +450,10 @@ def main():
     # roofline: algorithmic FLOPs per launch / launch time vs the measured FMA peak
     flops_ss = w.pattern.flops_per_step()
     achieved = flops_ss * sys_steps / (kernel_s / args.steps)
-    import ctypes
-    peak = ctypes.c_double()
-    N.check(N.lib.pasif_fma_peak(N.FP32, ctypes.byref(peak)))
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic_coupled2_fp32k.json")
     if os.path.exists(tp):
         traffic = json.load(open(tp)).get("dram_bytes_per_launch")
-    peak64 = ctypes.c_double()
-    N.check(N.lib.pasif_fma_peak(N.FP64, ctypes.byref(peak64)))
     fp64_achieved = flops_ss * sys_steps / fp64_s
     clocks = clk.summary()
     if rank == 0:

@@ -15,6 +15,9 @@
 //   F n <vals>   IC n <vals>
 //   has_bwd, then the same K G L P F IC blocks for the adjoint when 1
 //   task: 0 amplitudes | 1 trajectory <save> | 2 gradient <save>
+// An optional third argument names a file that receives the wall time of the
+// getter call in seconds (oracle/ref/time_ref.py).
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -57,7 +60,7 @@ static Sys read_sys() {
 }
 
 int main(int argc, char** argv) {
-    if (argc < 3) { std::fprintf(stderr, "usage: ref_driver case.txt out.txt\n"); return 2; }
+    if (argc < 3) { std::fprintf(stderr, "usage: ref_driver case.txt out.txt [seconds.txt]\n"); return 2; }
     g_in = std::fopen(argv[1], "r");
     if (!g_in) return 2;
     const size_t E = ru(), L = ru();
@@ -94,10 +97,17 @@ int main(int argc, char** argv) {
         d._allocateAdjointOnDevice();
     }
     std::vector<double> out;
+    const auto t0 = std::chrono::steady_clock::now();
     if (task == 0) out = d._getAmplitudes();
     else if (task == 1) out = d._getTrajectory(save);
     else out = d._getGradient(save);
     cudaError_t e = cudaDeviceSynchronize();
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (argc > 3) {   // wall time of the getter call (the whole solve, host loop included)
+        FILE* ft = std::fopen(argv[3], "w");
+        std::fprintf(ft, "%.9f\n", secs);
+        std::fclose(ft);
+    }
     FILE* fo = std::fopen(argv[2], "w");
     std::fprintf(fo, "%d %zu\n", (int)e, out.size());
     for (double v : out) std::fprintf(fo, "%.17g\n", v);

@@ -3,6 +3,7 @@
     python -m pasif_gb300.profile_cases fwd coupled2 [nsteps]
     python -m pasif_gb300.profile_cases fwd banded32
     python -m pasif_gb300.profile_cases adj chain8
+    python -m pasif_gb300.profile_cases fwd coupled2 20000 fp32_ext    (precision, default fp32_kahan)
 
 Each run compiles the kernel, makes one short warm-up launch, then one launch
 of the case (so `ncu -k regex:pk_fwd -s 1 -c 1` captures the case), and prints
@@ -56,4 +57,5 @@ def run(mode: str, case: str, nsteps: int | None = None, precision: str = "fp32_
 
 
 if __name__ == "__main__":
-    run(sys.argv[1], sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else None)
+    run(sys.argv[1], sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else None,
+        sys.argv[4] if len(sys.argv) > 4 else "fp32_kahan")

@@ -80,6 +80,19 @@ class Pattern:
         rhs = 2 * self.k_nnz + 3 * len(self.g_idx) + 4 * len(self.l_idx) + 5 * len(self.p_idx) + 2 * len(self.f_idx) + 3
         return 4 * rhs + 13 * self.n + 2 * reduced
 
+    def adjoint_flops_per_step(self, reduced: int = 0) -> int:
+        """Algorithmic FLOPs of one step of the exact discrete adjoint with
+        sqrt(N) checkpoints (FMA = 2): two forward steps (the checkpoint pass
+        and the chunk replay), the three stage inputs recomputed from the
+        step's state (3 right-hand sides + 2n each), and four vector-Jacobian
+        products, each with the parameter-gradient terms: per K entry 4
+        (one fma into the adjoint, one into the gradient), per Gamma entry 9,
+        Lambda 15, Psi 22, forcing 2; plus 10 n for the stage weights and the
+        adjoint update (+2 per component of a sum-of-squares loss)."""
+        rhs = 2 * self.k_nnz + 3 * len(self.g_idx) + 4 * len(self.l_idx) + 5 * len(self.p_idx) + 2 * len(self.f_idx) + 3
+        vjp = 4 * self.k_nnz + 9 * len(self.g_idx) + 15 * len(self.l_idx) + 22 * len(self.p_idx) + 2 * len(self.f_idx)
+        return 2 * self.flops_per_step() + 3 * (rhs + 2 * self.n) + 4 * vjp + 10 * self.n + 2 * reduced
+
     @staticmethod
     def from_dense_lists(n, k_rows, k_cols, g=(), l=(), p=(), f=(), n_sp=0):
         """Pattern from COO K entries (sorted into CSR order, stable) and tensor index lists.

@@ -764,26 +764,25 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             o << "  __device__ __forceinline__ void zero_pbar(double* pbar, long long B, int b) const {\n";
             for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = 0.0;\n";
             o << "  }\n";
-            // FP32 compensated per-chunk totals in global memory (sum at q, compensation at P + q)
-            const int Pt = pat.P();
-            o << "  template <class PV> __device__ __forceinline__ void add_pk(const PV& ps, R* pk, long long B, int b)"
-                 " const {\n";
+            // FP32 compensated per-chunk totals in shared memory: value q's sum
+            // at pk[64 q], its compensation at pk[64 q + 32] (pk holds the lane)
+            o << "  template <class PV> __device__ __forceinline__ void add_pk(const PV& ps, R* pk) const {\n";
             for (auto& kv : pslot)
-                o << "    { R s_ = pk[" << kv.first << "LL * B + b], c_ = pk[" << (Pt + kv.first)
-                  << "LL * B + b]; kahan_add(s_, c_, ps[" << kv.second << "]); pk[" << kv.first
-                  << "LL * B + b] = s_; pk[" << (Pt + kv.first) << "LL * B + b] = c_; }\n";
+                o << "    { R s_ = pk[" << 64 * kv.first << "], c_ = pk[" << 64 * kv.first + 32
+                  << "]; kahan_add(s_, c_, ps[" << kv.second << "]); pk[" << 64 * kv.first << "] = s_; pk["
+                  << 64 * kv.first + 32 << "] = c_; }\n";
             o << "  }\n";
             o << "  template <bool EXT> __device__ __forceinline__ void flush_pk(R* pk, double* pbar, long long B,"
                  " int b, double s) const {\n";
             for (auto& kv : pslot)
-                o << "    { const double t_ = (double)pk[" << kv.first << "LL * B + b] - (double)pk["
-                  << (Pt + kv.first) << "LL * B + b]; pbar[" << kv.first << "LL * B + b] = EXT ? M<double>::fma(s, t_, "
-                  << "pbar[" << kv.first << "LL * B + b]) : pbar[" << kv.first << "LL * B + b] + t_; pk["
-                  << kv.first << "LL * B + b] = R(0); pk[" << (Pt + kv.first) << "LL * B + b] = R(0); }\n";
+                o << "    { const double t_ = (double)pk[" << 64 * kv.first << "] - (double)pk[" << 64 * kv.first + 32
+                  << "]; pbar[" << kv.first << "LL * B + b] = EXT ? M<double>::fma(s, t_, pbar[" << kv.first
+                  << "LL * B + b]) : pbar[" << kv.first << "LL * B + b] + t_; pk[" << 64 * kv.first << "] = R(0); pk["
+                  << 64 * kv.first + 32 << "] = R(0); }\n";
             o << "  }\n";
-            o << "  __device__ __forceinline__ void zero_pk(R* pk, long long B, int b) const {\n";
+            o << "  __device__ __forceinline__ void zero_pk(R* pk) const {\n";
             for (auto& kv : pslot)
-                o << "    pk[" << kv.first << "LL * B + b] = R(0); pk[" << (Pt + kv.first) << "LL * B + b] = R(0);\n";
+                o << "    pk[" << 64 * kv.first << "] = R(0); pk[" << 64 * kv.first + 32 << "] = R(0);\n";
             o << "  }\n";
         }
         o << "};\n";
@@ -816,7 +815,20 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
         o << " } break;\n";
     }
     o << "    default: break;\n  }\n}\n";
-    o << "// ws-launch " << 32 * sl.L << " " << (adj ? 6 : 2) * sl.NP * 32 * (key.f32 ? 4 : 8) << "\n";
+    // FP32 adjoint with a slice holding more than 16 values: their compensated
+    // gradient totals in shared memory (ws_adj, PKREG false), 64 floats per value
+    size_t max_po = 0;
+    if (adj && key.f32) {
+        const auto dt2 = dest_terms(pat);
+        for (int w = 0; w < sl.L; ++w) {
+            size_t po = 0;
+            for (int i : sl.own[w]) po += dt2[i].size();
+            max_po = std::max(max_po, po);
+        }
+    }
+    const long long pk_floats = max_po > 16 ? 64LL * pat.P() : 0;
+    o << "// ws-launch " << 32 * sl.L << " " << ((adj ? 6 : 2) * sl.NP * 32 + pk_floats) * (key.f32 ? 4 : 8)
+      << "\n";
     return o.str();
 }
 
@@ -1243,6 +1255,8 @@ int ws_split(int n, bool f32, bool force, bool adjoint, bool ext) {
     int L = std::max(4, (n + cpw - 1) / cpw);
     if (adjoint && f32 && !force) L = std::min(L, 8);
     if (const char* e = std::getenv("PASIF_WS_SLICES")) L = std::atoi(e);   // tuning override
+    if (const char* e = std::getenv(adjoint ? "PASIF_WS_SLICES_ADJ" : "PASIF_WS_SLICES_FWD"))
+        L = std::atoi(e);   // tuning override of one kind of kernel
     return std::max(2, std::min(16, std::min(L, n)));
 }
 

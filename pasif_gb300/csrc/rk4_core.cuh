@@ -1437,6 +1437,10 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
     R* const r4 = sm + 3 * NP * 32;
     R* const k0 = sm + 4 * NP * 32;
     R* const k1 = sm + 5 * NP * 32;
+    // FP32 adjoints whose slices' gradient totals do not fit registers: the
+    // compensated per-chunk totals in shared memory after the six regions,
+    // two slots of 32 lanes per value (sum, compensation)
+    R* const pkm = sm + 6 * NP * 32;
     constexpr int SV = adj_slot_vecs<R>();
     sl.load(a.vals, B, b);
     const long long ebase = (long long)a.exc_index[b] * (long long)a.frc.len;
@@ -1527,9 +1531,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
         const int start = k * a.C;
         const int end = (start + a.C < a.nsteps) ? start + a.C : a.nsteps;
         const int slot0 = a.stored ? a.slot_base : start;   // buf slot of step t: t - slot0
-        if constexpr (STEP_ACC && !PKREG) {
-            if (valid) sl.zero_pk(a.pk, B, b);
-        }
+        if constexpr (STEP_ACC && !PKREG) sl.zero_pk(pkm);
         if (!a.stored) {
             const R* ck = a.ckpt + (long long)k * 2 * N * B;
             sl.load_vec(Q, ck, B, b);
@@ -1680,8 +1682,8 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                 if constexpr (PBREG) {
 #pragma unroll
                     for (int p = 0; p < PO; ++p) kahan_add(PK[p], PKC[p], pst[p]);
-                } else {   // the same compensated sums, in a.pk
-                    if (valid) sl.add_pk(pst, a.pk, B, b);
+                } else {   // the same compensated sums, in shared memory
+                    sl.add_pk(pst, pkm);
                 }
 #pragma unroll
                 for (int p = 0; p < PO; ++p) pst[p] = R(0);
@@ -1697,7 +1699,7 @@ __device__ __forceinline__ void ws_adj(SL& sl, const AdjArgs<R>& a, R* sm, int b
                 PKC[p] = R(0);
             }
         } else if constexpr (STEP_ACC) {
-            if (valid) sl.template flush_pk<EXT>(a.pk, a.pbar, B, b, h6d);
+            if (valid) sl.template flush_pk<EXT>(pkm, a.pbar, B, b, h6d);
         }
     }
     if (!valid) return;

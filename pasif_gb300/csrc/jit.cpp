@@ -200,6 +200,146 @@ struct Emitter {
         }
     }
 
+    // rhs body of the packed-FP32 forward kernels (thread per system, FP32,
+    // forward only: xs and xp are the same vector).  The operations and their
+    // order per destination are those of rhs() below -- the oracle's bits --
+    // but destinations 2m and 2m+1 are evaluated together: the k-th operation
+    // of a partial sum of one and the k-th of the same partial sum of the
+    // other become one f32x2 instruction (mul.rn / fma.rn / add.rn.f32x2, two
+    // independent correctly rounded results), as do the multiplications
+    // forming the terms' first factors, level by level.  What has no partner
+    // (a longer partial sum, a deeper product) stays scalar.  A value that is
+    // exactly 1 or -1 folds: 1*x = x, fma(1, x, s) = s + x, fma(-1, x, s) =
+    // s - x, all exact, so the bits do not change.
+    void rhs_pair(std::ostringstream& o, bool force) const {
+        const int n = pat.n;
+        const int go = pat.k_nnz(), lo = go + pat.g_nnz(), po = lo + pat.l_nnz(), fo = po + pat.p_nnz();
+        auto S = [](int v) { return std::to_string(v); };
+        struct T { std::string v; std::vector<int> ops; };   // value, state factors (none: the forcing term)
+        std::vector<std::vector<T>> terms(n);
+        for (int i = 0; i < n; ++i)
+            for (int q = pat.k_ptr[i]; q < pat.k_ptr[i + 1]; ++q) terms[i].push_back({val(q), {pat.k_col[q]}});
+        for (int e = 0; e < pat.g_nnz(); ++e) {
+            const int* ix = &pat.g_idx[3 * e];
+            terms[ix[0]].push_back({val(go + e), {ix[1], ix[2]}});
+        }
+        for (int e = 0; e < pat.l_nnz(); ++e) {
+            const int* ix = &pat.l_idx[4 * e];
+            terms[ix[0]].push_back({val(lo + e), {ix[1], ix[2], ix[3]}});
+        }
+        for (int e = 0; e < pat.p_nnz(); ++e) {
+            const int* ix = &pat.p_idx[5 * e];
+            terms[ix[0]].push_back({val(po + e), {ix[1], ix[2], ix[3], ix[4]}});
+        }
+        if (force)
+            for (int e = 0; e < pat.f_nnz(); ++e) terms[pat.f_idx[e]].push_back({val(fo + e), {}});
+        const std::string one = hexlit(1.0), mone = hexlit(-1.0);
+        auto X = [&](int c) { return "xs[" + S(c) + "]"; };
+        auto last_of = [&](const T& t) { return t.ops.empty() ? std::string("u") : X(t.ops.back()); };
+        auto depth = [](const T& t) { return t.ops.empty() ? 0 : (int)t.ops.size() - 1; };
+        // scalar first factor of t from level `from` on, given the factor so far
+        auto scalar_first = [&](const T& t, int from, std::string f) {
+            for (int l = from; l < depth(t); ++l) {
+                if (f == one) f = X(t.ops[l]);
+                else if (f == mone) f = "(-" + X(t.ops[l]) + ")";
+                else f = "m::mul(" + f + ", " + X(t.ops[l]) + ")";
+            }
+            return f;
+        };
+        // scalar operation k of a partial sum held in `acc`
+        auto scalar_op = [&](const std::string& acc, size_t k, const std::string& f, const std::string& l) {
+            if (k == 0) {
+                if (f == one) return acc + " = " + l + ";\n";
+                if (f == mone) return acc + " = -" + l + ";\n";
+                return acc + " = m::mul(" + f + ", " + l + ");\n";
+            }
+            if (f == one) return acc + " = m::add(" + acc + ", " + l + ");\n";
+            if (f == mone) return acc + " = m::sub(" + acc + ", " + l + ");\n";
+            return acc + " = m::fma(" + f + ", " + l + ", " + acc + ");\n";
+        };
+        auto P2 = [](const std::string& a, const std::string& b) { return "make_float2(" + a + ", " + b + ")"; };
+        int nf = 0;
+        for (int i = 0; i < n; i += 2) {
+            const int j = i + 1;
+            if (j >= n || terms[i].empty() || terms[j].empty()) {   // no partner: the scalar form
+                for (int d = i; d < std::min(n, i + 2); ++d) {
+                    if (terms[d].empty()) {
+                        o << "      f[" << d << "] = R(0);\n";
+                        continue;
+                    }
+                    o << "      {\n        R a" << (terms[d].size() >= 2 ? ", c" : "") << ";\n";
+                    for (size_t k = 0; k < terms[d].size(); ++k) {
+                        const T& t = terms[d][k];
+                        o << "        " << scalar_op((k & 1) ? "c" : "a", k / 2, scalar_first(t, 0, t.v), last_of(t));
+                    }
+                    o << "        f[" << d << "] = " << (terms[d].size() >= 2 ? "m::add(a, c)" : "a") << ";\n      }\n";
+                }
+                continue;
+            }
+            const size_t ni = terms[i].size(), nj = terms[j].size();
+            o << "      {\n        float2 pa" << (std::max(ni, nj) >= 2 ? ", pc" : "") << ";\n";
+            for (size_t k = 0; k < std::max(ni, nj); ++k) {
+                const std::string acc = (k & 1) ? "pc" : "pa";
+                const size_t pos = k / 2;
+                if (k < ni && k < nj) {
+                    const T& ti = terms[i][k];
+                    const T& tj = terms[j][k];
+                    std::string fi = ti.v, fj = tj.v;
+                    const int common = std::min(depth(ti), depth(tj));
+                    for (int l = 0; l < common; ++l) {
+                        if (fi == one && fj == one) {
+                            fi = X(ti.ops[l]);
+                            fj = X(tj.ops[l]);
+                            continue;
+                        }
+                        const std::string nm = "ff" + S(nf++);
+                        o << "        const float2 " << nm << " = M2::mul(" << P2(fi, fj) << ", "
+                          << P2(X(ti.ops[l]), X(tj.ops[l])) << ");\n";
+                        fi = nm + ".x";
+                        fj = nm + ".y";
+                    }
+                    fi = scalar_first(ti, common, fi);
+                    fj = scalar_first(tj, common, fj);
+                    const std::string L = P2(last_of(ti), last_of(tj));
+                    if (pos == 0) {
+                        // ptxas may contract a packed multiply with a packed or scalar add that
+                        // consumes it into one fma (rounding once instead of twice), whatever
+                        // the rounding modifiers: a packed product is only used as the addend
+                        // of the partial sum's next packed fma; otherwise two scalar products.
+                        const bool next_fma2 = k + 2 < ni && k + 2 < nj &&
+                                               !(depth(terms[i][k + 2]) == 0 && depth(terms[j][k + 2]) == 0 &&
+                                                 terms[i][k + 2].v == terms[j][k + 2].v &&
+                                                 (terms[i][k + 2].v == one || terms[i][k + 2].v == mone));
+                        if (fi == one && fj == one) o << "        " << acc << " = " << L << ";\n";
+                        else if (next_fma2) o << "        " << acc << " = M2::mul(" << P2(fi, fj) << ", " << L << ");\n";
+                        else {
+                            auto prod = [&](const std::string& f, const std::string& l) {
+                                return f == one ? l : f == mone ? "(-" + l + ")" : "m::mul(" + f + ", " + l + ")";
+                            };
+                            o << "        " << acc << " = " << P2(prod(fi, last_of(ti)), prod(fj, last_of(tj))) << ";\n";
+                        }
+                    } else {
+                        if (fi == one && fj == one) o << "        " << acc << " = M2::add(" << acc << ", " << L << ");\n";
+                        else if (fi == mone && fj == mone) o << "        " << acc << " = M2::sub(" << acc << ", " << L << ");\n";
+                        else o << "        " << acc << " = M2::fma(" << P2(fi, fj) << ", " << L << ", " << acc << ");\n";
+                    }
+                } else {   // only one destination has a k-th term
+                    const T& t = k < ni ? terms[i][k] : terms[j][k];
+                    const std::string lane = acc + (k < ni ? ".x" : ".y");
+                    o << "        " << scalar_op(lane, pos, scalar_first(t, 0, t.v), last_of(t));
+                }
+            }
+            if (ni >= 2 && nj >= 2) {
+                o << "        const float2 r = M2::add(pa, pc);\n";
+                o << "        f[" << i << "] = r.x;\n        f[" << j << "] = r.y;\n";
+            } else {
+                o << "        f[" << i << "] = " << (ni >= 2 ? "m::add(pa.x, pc.x)" : "pa.x") << ";\n";
+                o << "        f[" << j << "] = " << (nj >= 2 ? "m::add(pa.y, pc.y)" : "pa.y") << ";\n";
+            }
+            o << "      }\n";
+        }
+    }
+
     // rhs body.  Per destination, the terms [K row | Gamma | Lambda | Psi |
     // forcing] are dealt in turn to two partial sums (a, c), each fma-folded
     // from +0, and added when both are used: the canonical order of the
@@ -863,22 +1003,54 @@ static void emit_sample_ring(std::ostringstream& o, int W, int block, const Patt
 }
 
 namespace {
-void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32, bool fast = false);
+void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32, bool fast = false,
+                   bool pair = false);
+}
+
+// Packed-FP32 (f32x2) form of the thread-per-system forward (rk4_step's
+// PAIR): 0 = scalar, 1 = packed stages with a scalar compensated update,
+// 2 = packed update too; the bits are the same in every form.  Chosen from
+// GB300 measurements of the forward (16384 systems; scalar -> packed):
+// plain FP32 gains wherever a destination pair 2m, 2m+1 has work on both
+// sides (2-DOF coupled +45 %, 4-DOF chain +17 %); with the compensated update
+// only small dense systems gain (2-DOF coupled, n = 5, two coupled rows of 8
+// terms: +13.5 %), spring chains lose (n = 4, 8, 16: -3 to -19 %: their rows
+// pair with shifted columns, so most packed operands must be assembled), so
+// compensated forwards are packed only for n <= 6 with a destination pair of
+// at least 4 terms on each side.  PASIF_FP32X2 overrides the choice (tuning).
+int fwd_paired(const Pattern& pat, const FwdKernelKey& key) {
+    if (!key.f32 || key.ext || key.fast || key.slices >= 2) return 0;
+    std::vector<int> cnt(pat.n, 0);
+    for (int i = 0; i < pat.n; ++i) cnt[i] = pat.k_ptr[i + 1] - pat.k_ptr[i];
+    for (int e = 0; e < pat.g_nnz(); ++e) ++cnt[pat.g_idx[3 * e]];
+    for (int e = 0; e < pat.l_nnz(); ++e) ++cnt[pat.l_idx[4 * e]];
+    for (int e = 0; e < pat.p_nnz(); ++e) ++cnt[pat.p_idx[5 * e]];
+    int both = 0, dense = 0;
+    for (int i = 0; i + 1 < pat.n; i += 2) {
+        both += cnt[i] > 0 && cnt[i + 1] > 0;
+        dense += cnt[i] >= 4 && cnt[i + 1] >= 4;
+    }
+    if (both == 0) return 0;
+    int mode = !key.kahan ? 2 : (pat.n <= 6 && dense > 0) ? 2 : 0;
+    if (const char* e = std::getenv("PASIF_FP32X2")) mode = std::max(0, std::min(2, std::atoi(e)));
+    return mode;
 }
 
 std::string fwd_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key) {
     if (key.slices >= 2) return ws_source(pat, lit, key, 0);
     Emitter em(pat, lit, key.ext);
     const int n = pat.n;
+    const int pair = fwd_paired(pat, key);
     std::ostringstream o;
     o << "// generated by pasif_gb300 jit.cpp: forward RK4, n=" << n << " P=" << pat.P()
-      << (key.ext ? " extended state" : "") << (key.fast ? " fast" : "") << "\n";
-    emit_sys_head(o, pat, em, key.f32, key.fast);
+      << (key.ext ? " extended state" : "") << (key.fast ? " fast" : "") << (pair ? " packed FP32" : "") << "\n";
+    emit_sys_head(o, pat, em, key.f32, key.fast, pair > 0);
     o << "};\n";
     // forcing window and weights as compile-time constants
     const int W = key.window;
     o << "struct JW {\n  static constexpr int W = " << W << ";\n";
     o << "  static constexpr bool FAST = " << (key.fast ? "true" : "false") << ";\n";
+    o << "  static constexpr int PAIR = " << pair << ";\n";
     emit_sample_ring(o, W, key.block, pat);
     for (int which = 0; which < 2; ++which) {
         o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";
@@ -910,7 +1082,7 @@ bool fwd_compile_report(const Pattern& pat, const Literals& lit, const FwdKernel
 namespace {
 
 // JSys members shared by the forward and adjoint programs: values, load, rhs.
-void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32, bool fast) {
+void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em, bool f32, bool fast, bool pair) {
     o << "#include \"rk4_core.cuh\"\n";
     o << "namespace pk {\n";
     o << "typedef " << (f32 ? "float" : "double") << " R;\n";
@@ -934,6 +1106,16 @@ void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em,
     }
     o << "  template <bool FORCE, class V, class W, class F>\n";
     o << "  __device__ __forceinline__ void rhs(const V& xs, const W& xp, R u, F& f) const {\n";
+    if (pair) {   // packed-FP32 forward: xs and xp are the same vector
+        o << "    typedef M<R> m;\n    (void)xp;\n";
+        o << "    if (FORCE) {\n";
+        em.rhs_pair(o, true);
+        o << "    } else {\n";
+        em.rhs_pair(o, false);
+        o << "    }\n";
+        o << "  }\n";
+        return;
+    }
     if (fast) {   // forward systems only: xs and xp are the same vector
         o << "    typedef M<R> m;\n    (void)xp;\n";
         o << "    if (FORCE) {\n";
@@ -1164,6 +1346,7 @@ std::string pool_source(const Pattern& pat, const FwdKernelKey& key) {
     const int W = key.window;
     o << "struct JW {\n  static constexpr int W = " << W << ";\n";
     o << "  static constexpr bool FAST = false;\n";
+    o << "  static constexpr int PAIR = 0;\n";
     emit_sample_ring(o, W, key.block, pat);
     for (int which = 0; which < 2; ++which) {
         o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";

@@ -38,6 +38,58 @@ template <> struct M<float> {
     static __device__ __forceinline__ float max(float a, float b) { return fmaxf(a, b); }
 };
 
+// Packed FP32 (f32x2) arithmetic: two independent correctly rounded FP32
+// operations in one instruction (sm_100 and later).  Each lane's result is
+// the scalar __fmaf_rn / __fmul_rn / __fadd_rn / __fsub_rn of its operands,
+// so code written with it keeps the bits of the scalar code.
+#ifndef PK_HOST_EMU
+// Inline PTX with explicit .rn modifiers.  Measured on GB300 (CUDA 13.0):
+// ptxas still contracts a packed multiply (mul.rn.f32x2, or fma.rn.f32x2
+// with a -0 addend) whose result feeds a packed subtract into one fma, which
+// rounds once instead of twice; a scalar mul.rn.f32 is never contracted.  So
+// a packed product is only ever used as a factor or as the addend of another
+// packed fma; products that feed an add or subtract are scalar.
+struct M2 {
+    static __device__ __forceinline__ unsigned long long pack(float2 a) {
+        unsigned long long r;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+        return r;
+    }
+    static __device__ __forceinline__ float2 unpack(unsigned long long r) {
+        float2 o;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(o.x), "=f"(o.y) : "l"(r));
+        return o;
+    }
+    static __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) {
+        unsigned long long r;
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pack(a)), "l"(pack(b)), "l"(pack(c)));
+        return unpack(r);
+    }
+    static __device__ __forceinline__ float2 mul(float2 a, float2 b) {
+        unsigned long long r;
+        asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack(a)), "l"(pack(b)));
+        return unpack(r);
+    }
+    static __device__ __forceinline__ float2 add(float2 a, float2 b) {
+        unsigned long long r;
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack(a)), "l"(pack(b)));
+        return unpack(r);
+    }
+    static __device__ __forceinline__ float2 sub(float2 a, float2 b) {
+        unsigned long long r;
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack(a)), "l"(pack(b)));
+        return unpack(r);
+    }
+};
+#else
+struct M2 {
+    static inline float2 fma(float2 a, float2 b, float2 c) { return make_float2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y)); }
+    static inline float2 mul(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+    static inline float2 add(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
+    static inline float2 sub(float2 a, float2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
+};
+#endif
+
 // L2 prefetch of the line holding p (an address inside an allocation): the
 // backward sweep over a stored trajectory reads states written long before,
 // from HBM; prefetched kPrefetchSteps steps ahead they are in L2 when needed.
@@ -301,14 +353,102 @@ struct GenSys {
 // h/6 k1 - c + h/3 k2 + h/3 k3 + h/6 k4 directly (the compensation folded into
 // its first fma, h/3 = 2 h6 exactly) instead of h/6 ((k1 + 2k2) + 2k3 + k4) - c:
 // the same compensated update in fewer operations, not the oracle's bits.
-template <typename R, int N, bool KAHAN, int NSTG = 0, bool EXT = false, bool FAST = false, class Sys, class V>
+// PAIR (packed-FP32 kernels, FP32 forward with a paired right-hand side):
+// the same operations in the same order, components 2m and 2m+1 updated
+// together by f32x2 instructions (M2): the bits of the scalar step.  PAIR 1
+// leaves the compensated (Kahan) update scalar, PAIR 2 packs it too.
+template <typename R, int N, bool KAHAN, int NSTG = 0, bool EXT = false, bool FAST = false, int PAIR = 0,
+          class Sys, class V>
 __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K, V& Mi,
                                          R ua, R ub, R uc, R h, R h2, R h6, R* stg = nullptr, long long sB = 0,
                                          R h6lo = R(0)) {
     typedef M<R> m;
     static_assert(!EXT || N > 0, "extended-state steps need a compile-time state size");
     static_assert(!FAST || (!EXT && NSTG == 0), "fast steps are plain forward steps");
+    static_assert(!PAIR || (sizeof(R) == 4 && N > 0 && !EXT && !FAST && NSTG <= 1), "paired steps: FP32 forward");
     const int n = N ? N : sys.dim();
+    if constexpr (PAIR) {
+        typedef M2 p2;
+        auto P = [](R x, R y) { return make_float2(x, y); };
+        const float2 H2 = P(h2, h2), H = P(h, h), TWO = P(R(2), R(2)), H6 = P(h6, h6);
+        if constexpr (NSTG >= 1) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) stg[i * sB] = Q[i];
+        }
+        sys.template rhs<true>(Q, Q, ua, K);
+#pragma unroll
+        for (int i = 0; i + 1 < N; i += 2) {
+            S[i] = K[i];
+            S[i + 1] = K[i + 1];
+            const float2 r = p2::fma(H2, P(K[i], K[i + 1]), P(Q[i], Q[i + 1]));
+            Mi[i] = r.x;
+            Mi[i + 1] = r.y;
+        }
+        if constexpr (N & 1) { S[N - 1] = K[N - 1]; Mi[N - 1] = m::fma(h2, K[N - 1], Q[N - 1]); }
+#pragma unroll
+        for (int stage = 0; stage < 2; ++stage) {
+            sys.template rhs<true>(Mi, Mi, ub, K);
+            const float2 HS = stage == 0 ? H2 : H;
+#pragma unroll
+            for (int i = 0; i + 1 < N; i += 2) {
+                const float2 k = P(K[i], K[i + 1]);
+                const float2 s = p2::fma(TWO, k, P(S[i], S[i + 1]));
+                const float2 r = p2::fma(HS, k, P(Q[i], Q[i + 1]));
+                S[i] = s.x;
+                S[i + 1] = s.y;
+                Mi[i] = r.x;
+                Mi[i + 1] = r.y;
+            }
+            if constexpr (N & 1) {
+                S[N - 1] = m::fma(R(2), K[N - 1], S[N - 1]);
+                Mi[N - 1] = m::fma(stage == 0 ? h2 : h, K[N - 1], Q[N - 1]);
+            }
+        }
+        sys.template rhs<true>(Mi, Mi, uc, K);
+        if constexpr (KAHAN && PAIR == 1) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const R y = m::sub(m::mul(h6, m::add(S[i], K[i])), Cm[i]);
+                const R t = m::add(Q[i], y);
+                Cm[i] = m::sub(m::sub(t, Q[i]), y);
+                Q[i] = t;
+            }
+            return;
+        }
+#pragma unroll
+        for (int i = 0; i + 1 < N; i += 2) {
+            const float2 sum = p2::add(P(S[i], S[i + 1]), P(K[i], K[i + 1]));
+            const float2 q = P(Q[i], Q[i + 1]);
+            float2 t;
+            if constexpr (KAHAN) {
+                const float2 c = P(Cm[i], Cm[i + 1]);
+                // scalar products: ptxas would contract a packed multiply into the
+                // packed subtract that consumes it (one rounding instead of two)
+                const float2 y = p2::sub(P(m::mul(h6, sum.x), m::mul(h6, sum.y)), c);
+                t = p2::add(q, y);
+                const float2 cn = p2::sub(p2::sub(t, q), y);
+                Cm[i] = cn.x;
+                Cm[i + 1] = cn.y;
+            } else {
+                t = p2::fma(H6, sum, q);
+            }
+            Q[i] = t.x;
+            Q[i + 1] = t.y;
+        }
+        if constexpr (N & 1) {
+            const int i = N - 1;
+            const R sum = m::add(S[i], K[i]);
+            if constexpr (KAHAN) {
+                const R y = m::sub(m::mul(h6, sum), Cm[i]);
+                const R t = m::add(Q[i], y);
+                Cm[i] = m::sub(m::sub(t, Q[i]), y);
+                Q[i] = t;
+            } else {
+                Q[i] = m::fma(h6, sum, Q[i]);
+            }
+        }
+        return;
+    }
     if constexpr (FAST) {
         const R h3 = m::add(h6, h6);
         sys.template rhs<true>(Q, Q, ua, K);
@@ -508,6 +648,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     typedef M<R> m;
     constexpr int W = WP::W;
     constexpr bool FASTK = WP::FAST && HTRAJ == 0 && !EXT;   // fast steps: plain forwards only
+    constexpr int PAIRK = (WP::PAIR && !EXT && !FASTK) ? WP::PAIR : 0;   // paired (f32x2) steps: FP32 forwards
     constexpr unsigned SPI = W == 0 ? 1u : (unsigned)(W / 2);
     constexpr int STG = HTRAJ == 2 ? adj_slot_vecs<R>() : 0;
     const long long B = a.B;
@@ -563,7 +704,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     const unsigned end = rc.step0 + rc.nsteps;
     while (s < end && (s % SPI) != 0u) {
         pre(s);
-        rk4_step<R, N, KAHAN, STG, EXT, FASTK>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
+        rk4_step<R, N, KAHAN, STG, EXT, FASTK, PAIRK>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
                                                force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h,
                                                a.h2, a.h6, slot(s), B, a.h6lo);
         post(s);
@@ -612,7 +753,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
                     else un = g1 ? m::fma(WP::wc(0), x1, m::mul(WP::wn(0), x2)) : R(0);
                 }
                 pre(s + (unsigned)r);
-                rk4_step<R, N, KAHAN, STG, EXT, FASTK>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6,
+                rk4_step<R, N, KAHAN, STG, EXT, FASTK, PAIRK>(sys, Q, Cm, S, K, Mi, ua, ub, un, a.h, a.h2, a.h6,
                                                        slot(s + (unsigned)r), B, a.h6lo);
                 post(s + (unsigned)r);
                 uc = un;
@@ -625,7 +766,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     }
     while (s < end) {
         pre(s);
-        rk4_step<R, N, KAHAN, STG, EXT, FASTK>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
+        rk4_step<R, N, KAHAN, STG, EXT, FASTK, PAIRK>(sys, Q, Cm, S, K, Mi, force_at(frc, ebase, s, 0u, 0u),
                                                force_at(frc, ebase, s, 0u, 1u), force_at(frc, ebase, s, 1u, 0u), a.h,
                                                a.h2, a.h6, slot(s), B, a.h6lo);
         post(s);

@@ -29,6 +29,8 @@ static inline float __fmaf_rn(float a, float b, float c) { return std::fmaf(a, b
 static inline float __fmul_rn(float a, float b) { return a * b; }
 static inline float __fadd_rn(float a, float b) { return a + b; }
 static inline float __fsub_rn(float a, float b) { return a - b; }
+struct float2 { float x, y; };
+static inline float2 make_float2(float x, float y) { return float2{x, y}; }
 using std::fabs;
 using std::fmax;
 struct EmuDim { unsigned x, y, z; };

@@ -49,6 +49,49 @@ def test_forward_bit_exact_random_patterns(gpu, prec, generic, seed):
     np.testing.assert_array_equal(sq, osq)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("prec", ["fp32", "fp32_kahan"])
+@pytest.mark.parametrize("seed", range(4))
+def test_packed_fp32_forward_bit_exact(gpu, monkeypatch, mode, prec, seed):
+    """Packed-FP32 (f32x2) forward kernels forced on random patterns (mode 1:
+    packed stages, scalar compensated update; 2: packed update too), K values
+    of exactly 1 and -1 folded as literals, reducers on: equal to the oracle
+    bit for bit (ptxas must not contract a packed product into an add)."""
+    monkeypatch.setenv("PASIF_FP32X2", str(mode))
+    rng = np.random.default_rng(700 + seed)
+    pat, v = cases.random_system(rng, n=[2, 3, 5, 6][seed])
+    B, E, L = 96, 3, 90
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    vals[:, 0], vals[:, 1] = 1.0, -1.0
+    x = cases.signals(rng, E, L)
+    exc = rng.integers(0, E, B)
+    W = [0, 2, 8, 4][seed]
+    im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
+    src = Plan(pat, prec).jit_report(vals, window=W, im=im)
+    assert "packed FP32" in src.split("// ---- source ----\n", 1)[1].splitlines()[0]
+    red = dict(max_comp=[0], max_start=40, sq_comp=sorted({0, pat.n - 1}), sq_start=10)
+    st, mx, sq, info = run_gpu(pat, vals, x0, exc, x, 0.05, 120, W, im, prec, False, 5, **red)
+    assert info["kind"] == "specialised"
+    ost, omx, osq = O.batch_forward(pat, vals, x0, exc, x, 0.05, 120, W, im, prec, 5, **red)
+    np.testing.assert_array_equal(st, ost)
+    np.testing.assert_array_equal(mx, omx)
+    np.testing.assert_array_equal(sq, osq)
+
+
+def test_packed_fp32_config2_default(gpu):
+    """Config 2 in FP32 with compensated update compiles to the packed kernel
+    by default, and its states equal the oracle's bit for bit over 20000
+    steps (every forcing interval, the L2-resident table)."""
+    w = synth.coupled2(n_sys=512, nsteps=20_000)
+    src = Plan(w.pattern, "fp32_kahan").jit_report(w.values, window=w.window, im=w.im)
+    assert "packed FP32" in src.split("// ---- source ----\n", 1)[1].splitlines()[0]
+    st, mx, sq, info = run_gpu(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
+                               "fp32_kahan", **w.forward_kwargs())
+    ost, omx, osq = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
+                                    "fp32_kahan", 0, **w.forward_kwargs())
+    np.testing.assert_array_equal(st, ost)
+
+
 @pytest.mark.parametrize("name", ["duffing", "coupled2", "chain8", "banded32"])
 def test_configs_small_bit_exact(gpu, name):
     kw = {"duffing": dict(n_sys=200, nsteps=3000), "coupled2": dict(n_sys=256, nsteps=4000),

@@ -97,6 +97,29 @@ def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps,
     np.testing.assert_array_equal(got, ref)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("prec", ["fp32", "fp32_kahan"])
+@pytest.mark.parametrize("seed", range(3))
+def test_packed_fp32_kernel_matches_oracle(tmp_path, monkeypatch, mode, prec, seed):
+    """Packed-FP32 (f32x2) forward, forced on random patterns (mode 1:
+    packed stages and scalar compensated update, 2: packed update too), with
+    K values of exactly 1 and -1 folded as literals: the oracle's bits."""
+    monkeypatch.setenv("PASIF_FP32X2", str(mode))
+    rng = np.random.default_rng(900 + seed)
+    pat, v = cases.random_system(rng, n=[2, 5, 6][seed])
+    vals, x0 = cases.random_batch(rng, pat, v, 40)
+    vals[:, 0], vals[:, 1] = 1.0, -1.0
+    x = cases.signals(rng, 3, 28)
+    exc = rng.integers(0, 3, 40)
+    W = 8
+    im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W])
+    src = Plan(pat, prec).jit_report(vals, window=W, im=im)
+    assert "packed FP32" in src.split("// ---- source ----\n", 1)[1].splitlines()[0]
+    got = run_emulated(tmp_path, pat, vals, x0, exc, x, W, im, 0.05, 3, 61, prec)
+    ref, _, _ = O.batch_forward(pat, vals, x0, exc, x, 0.05, 61, W, im, prec, 3)
+    np.testing.assert_array_equal(got, ref)
+
+
 def run_emulated_adjoint(d, pat, prec, slicing, vals, x0, exc, x, im, gf, gs, N, sq, sq_start, h=0.03, split=0,
                          stored=False):
     """split > 0: run it as the split launches of Batch::adjoint with `split`

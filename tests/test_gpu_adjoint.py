@@ -59,9 +59,11 @@ def test_adjoint_config3_fd_and_fp32(gpu):
             out.append(b.get()[2][0])
         fd = (out[0] - out[1]) / (2 * eps)
         assert dv[0, q] == pytest.approx(fd, rel=1e-6, abs=1e-9)
-    dv32, _ = gpu_adjoint(*args, "fp32_kahan", None, gs, w.sq_comp, w.sq_start)
-    rel = np.abs(dv32 - dv) / (np.abs(dv) + 1e-3 * np.abs(dv).max())
-    assert rel.max() < 1e-4
+    # FP32 modes against FP64, per value relative to the system's largest gradient: within 1e-5
+    for prec in ("fp32_kahan", "fp32_ext"):
+        dv32, _ = gpu_adjoint(*args, prec, None, gs, w.sq_comp, w.sq_start)
+        rel = np.max(np.abs(dv32 - dv), axis=1) / np.max(np.abs(dv), axis=1)
+        assert rel.max() <= 1e-5, (prec, rel.max())
 
 
 @pytest.mark.parametrize("seed", range(3))
@@ -105,26 +107,38 @@ def test_adjoint_warp_sliced_fp32_equals_thread(gpu, nd):
     np.testing.assert_array_equal(out[0][1], out[1][1])
 
 
-def test_adjoint_fp32_kahan_within_bound(gpu):
-    """FP32-Kahan adjoint (compensated state and adjoint-state updates, per-step
-    FP32 gradient sums into FP64 totals) against the FP64 adjoint on the 8-DOF
-    chain, per system max|g32 - g64| / max|g64|: median <= 1e-6, every
-    system <= 5e-5 (measured on GB300: median ~1.5e-7, worst of 256 systems
-    1.2e-5; the worst systems are the ones whose 20000-step trajectories are
-    the most sensitive, the FP32 state itself differs from FP64 by ~1e-7).
-    The generic kernel performs the same adjoint-state operations: its d x0
-    equals the specialised kernels' bit for bit."""
+def test_adjoint_fp32_within_bound(gpu):
+    """FP32 adjoints against the FP64 adjoint on 256 8-DOF chains x 20000
+    steps, per system max|g32 - g64| / max|g64|.  FP32-Kahan (compensated
+    state and adjoint-state updates, per-step FP32 gradient sums into
+    compensated totals): median <= 1e-6, at most 2 % of the systems above
+    1e-5 (the ones whose trajectories amplify the FP32 rounding of the values
+    and of h/6).  The extended-state mode removes those two roundings: every
+    system <= 1e-5.  verified_adjoint (cross-check, FP64 recompute of the
+    flagged systems): every system <= 1e-5.  The generic kernel performs the
+    same adjoint-state operations: its d x0 equals the specialised kernels'
+    bit for bit."""
+    from pasif_gb300.batch import verified_adjoint
     w = synth.chain8(n_sys=256, nsteps=20_000)
     out = {}
-    for prec, generic in (("fp32_kahan", False), ("fp32_kahan", True), ("fp64", False)):
+    for prec, generic in (("fp32_kahan", False), ("fp32_kahan", True), ("fp32_ext", False), ("fp64", False)):
         plan = Plan(w.pattern, prec, generic_only=generic)
         b = Batch(plan, w.values, w.x0, w.exc_index)
         out[(prec, generic)] = b.adjoint(Signals(w.signals, w.window, w.im, prec), w.h, w.nsteps,
                                          g_sq=np.ones(w.n_sys), sq_comp=w.sq_comp, sq_start=w.sq_start)
-    g32, g64 = out[("fp32_kahan", False)][0], out[("fp64", False)][0]
-    err = np.max(np.abs(g32 - g64), axis=1) / np.max(np.abs(g64), axis=1)
-    assert np.median(err) <= 1e-6, np.median(err)
-    assert err.max() <= 5e-5, err.max()
+    g64 = out[("fp64", False)][0]
+
+    def err(g):
+        return np.max(np.abs(g - g64), axis=1) / np.max(np.abs(g64), axis=1)
+
+    e32 = err(out[("fp32_kahan", False)][0])
+    assert np.median(e32) <= 1e-6, np.median(e32)
+    assert (e32 > 1e-5).sum() <= 0.02 * w.n_sys, (e32 > 1e-5).sum()
+    eext = err(out[("fp32_ext", False)][0])
+    assert eext.max() <= 1e-5, eext.max()
+    gv, _, _ = verified_adjoint(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
+                                g_sq=np.ones(w.n_sys), sq_comp=w.sq_comp, sq_start=w.sq_start)
+    assert err(gv).max() <= 1e-5, err(gv).max()
     np.testing.assert_array_equal(out[("fp32_kahan", False)][1], out[("fp32_kahan", True)][1])
 
 

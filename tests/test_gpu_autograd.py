@@ -1,6 +1,7 @@
 """torch.autograd.Function: gradients through the adjoint kernel equal the
 oracle's exact discrete adjoint (FP64, bit for bit) and match finite
-differences of the forward; FP32-Kahan gradients within 1e-4 of FP64."""
+differences of the forward; FP32-Kahan and extended-state gradients within
+1e-5 of FP64 (per system, relative to its largest gradient)."""
 import numpy as np
 import pytest
 
@@ -28,12 +29,14 @@ def test_autograd_chain8(gpu):
                                w.im, g_final=gf, g_sq=wts.cpu().numpy(), sq_comp=w.sq_comp, sq_start=w.sq_start)
     np.testing.assert_array_equal(values.grad.cpu().numpy(), odv)
     np.testing.assert_array_equal(x0.grad.cpu().numpy(), odx)
-    # FP32 with compensated update
-    v32 = torch.tensor(w.values, device="cuda", requires_grad=True)
-    s32 = RK4Solver(w.pattern, w.signals, w.window, w.im, w.h, w.nsteps, w.exc_index, "fp32_kahan", w.sq_comp,
-                    w.sq_start)
-    st32, sq32 = s32(v32, torch.tensor(w.x0 + 0.01, device="cuda"))
-    ((sq32 * wts).sum() + 0.3 * st32[:, 0].sum()).backward()
-    g32, g64 = v32.grad.cpu().numpy(), values.grad.cpu().numpy()
-    rel = np.abs(g32 - g64) / (np.abs(g64) + 1e-3 * np.abs(g64).max())
-    assert rel.max() < 1e-4
+    # FP32 with compensated update, and the extended-state mode
+    g64 = values.grad.cpu().numpy()
+    for prec in ("fp32_kahan", "fp32_ext"):
+        v32 = torch.tensor(w.values, device="cuda", requires_grad=True)
+        s32 = RK4Solver(w.pattern, w.signals, w.window, w.im, w.h, w.nsteps, w.exc_index, prec, w.sq_comp,
+                        w.sq_start)
+        st32, sq32 = s32(v32, torch.tensor(w.x0 + 0.01, device="cuda"))
+        ((sq32 * wts).sum() + 0.3 * st32[:, 0].sum()).backward()
+        g32 = v32.grad.cpu().numpy()
+        rel = np.max(np.abs(g32 - g64), axis=1) / np.max(np.abs(g64), axis=1)
+        assert rel.max() <= 1e-5, (prec, rel.max())

@@ -12,6 +12,7 @@
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -581,6 +582,140 @@ Slicing make_slicing(const Pattern& pat, const std::vector<std::vector<Term>>& d
     return s;
 }
 
+// Slices whose structs are translates of one another share one struct.
+// Each slice's struct text comes with hooks \x01 <kind> <value> \x02 for
+// its slice-dependent numbers (ws_source): component indices (N), published
+// offsets (P), offsets of the compensated gradient totals (G), ranks of the
+// max-tracked components (R), all of which must move by one constant per
+// kind from slice to slice, and value indices (Q), which may move
+// arbitrarily.  Slices with the same text apart from the hooks, and constant
+// moves, form a group: one struct (the first member's), whose N/P/G/R
+// numbers become runtime bases plus the first member's numbers and whose Q
+// numbers are read from a per-warp table.  The warps of a group then run
+// the same instructions: with one struct per warp the SM's instruction
+// cache does not hold the code of all the warps of a block (GB300, 128-state
+// chain adjoint, 8 warps: 13 "no instruction" stalls per issued
+// instruction).  The operations are unchanged.
+struct SliceGroup {
+    int ref = 0;
+    std::vector<int> members;
+    std::vector<std::array<long long, 4>> shift;   // per member: N, P, G, R
+    std::vector<std::vector<long long>> q;          // per member: the Q numbers in text order
+};
+
+std::vector<SliceGroup> share_slices(const std::vector<std::string>& src, std::ostringstream& o) {
+    struct Code { std::string tmpl; std::vector<std::pair<char, long long>> hooks; };
+    std::vector<Code> code(src.size());
+    for (size_t w = 0; w < src.size(); ++w) {
+        const std::string& t = src[w];
+        for (size_t i = 0; i < t.size(); ++i) {
+            if (t[i] != '\x01') { code[w].tmpl += t[i]; continue; }
+            const size_t j = t.find('\x02', i);
+            code[w].hooks.push_back({t[i + 1], std::stoll(t.substr(i + 2, j - i - 2))});
+            code[w].tmpl += '\x01';
+            code[w].tmpl += t[i + 1];
+            i = j;
+        }
+    }
+    auto kind_index = [](char k) { return k == 'N' ? 0 : k == 'P' ? 1 : k == 'G' ? 2 : k == 'R' ? 3 : -1; };
+    bool share = true;
+    if (const char* e = std::getenv("PASIF_WS_SHARE")) share = std::atoi(e) != 0;   // tuning override
+    std::vector<SliceGroup> groups;
+    for (int w = 0; w < (int)src.size(); ++w) {
+        bool placed = false;
+        for (SliceGroup& g : groups) {
+            if (!share) break;
+            const Code& r = code[g.ref];
+            if (r.tmpl != code[w].tmpl) continue;
+            std::array<long long, 4> sh{};
+            std::array<bool, 4> set{};
+            std::vector<long long> qv;
+            bool ok = true;
+            for (size_t h = 0; h < r.hooks.size() && ok; ++h) {
+                const int k = kind_index(r.hooks[h].first);
+                const long long d = code[w].hooks[h].second - r.hooks[h].second;
+                if (k < 0) { qv.push_back(code[w].hooks[h].second); continue; }
+                if (!set[k]) { set[k] = true; sh[k] = d; }
+                else ok = sh[k] == d;
+            }
+            if (!ok) continue;
+            g.members.push_back(w);
+            g.shift.push_back(sh);
+            g.q.push_back(qv);
+            placed = true;
+            break;
+        }
+        if (placed) continue;
+        SliceGroup g;
+        g.ref = w;
+        g.members.push_back(w);
+        g.shift.push_back({0, 0, 0, 0});
+        std::vector<long long> qv;
+        for (const auto& hk : code[w].hooks)
+            if (kind_index(hk.first) < 0) qv.push_back(hk.second);
+        g.q.push_back(qv);
+        groups.push_back(g);
+    }
+    for (const SliceGroup& g : groups) {
+        const Code& c = code[g.ref];
+        const bool shared = g.members.size() > 1;
+        const std::string name = "SL" + std::to_string(g.ref);
+        size_t h = 0, qi = 0;
+        std::string body;
+        for (size_t i = 0; i < c.tmpl.size(); ++i) {
+            const char ch = c.tmpl[i];
+            if (ch == '\x03') { body += name; continue; }
+            if (ch == '\x04') {
+                if (shared) body += "  long long nb_ = 0; int pb_ = 0, gb_ = 0, rb_ = 0; const int* qt_ = nullptr;\n";
+                continue;
+            }
+            if (ch != '\x01') { body += ch; continue; }
+            const char kind = c.tmpl[++i];
+            const long long v = c.hooks[h++].second;
+            if (!shared) { body += std::to_string(v); continue; }
+            switch (kind) {
+                case 'N': body += "(nb_ + " + std::to_string(v) + ")"; break;
+                case 'P': body += "(pb_ + " + std::to_string(v) + ")"; break;
+                case 'G': body += "(gb_ + " + std::to_string(v) + ")"; break;
+                case 'R': body += "(rb_ + " + std::to_string(v) + ")"; break;
+                default: body += "qt_[" + std::to_string(qi++) + "]"; break;
+            }
+        }
+        o << body;
+        if (!shared) continue;
+        // per-warp bases and value indices of the group's members (other rows unused)
+        const int L = (int)src.size();
+        const size_t nq = std::max<size_t>(g.q[0].size(), 1);
+        o << "__device__ const long long " << name << "_NB[" << L << "] = {";
+        for (int w = 0; w < L; ++w) {
+            long long v = 0;
+            for (size_t m = 0; m < g.members.size(); ++m)
+                if (g.members[m] == w) v = g.shift[m][0];
+            o << (w ? ", " : "") << v;
+        }
+        o << "};\n";
+        o << "__device__ const int " << name << "_PGR[" << L << "][3] = {";
+        for (int w = 0; w < L; ++w) {
+            std::array<long long, 4> sh{};
+            for (size_t m = 0; m < g.members.size(); ++m)
+                if (g.members[m] == w) sh = g.shift[m];
+            o << (w ? ", " : "") << "{" << sh[1] << ", " << sh[2] << ", " << sh[3] << "}";
+        }
+        o << "};\n";
+        o << "__device__ const int " << name << "_QT[" << L << "][" << nq << "] = {";
+        for (int w = 0; w < L; ++w) {
+            const std::vector<long long>* qv = nullptr;
+            for (size_t m = 0; m < g.members.size(); ++m)
+                if (g.members[m] == w) qv = &g.q[m];
+            o << (w ? ", " : "") << "{";
+            for (size_t k = 0; k < nq; ++k) o << (k ? ", " : "") << (qv && k < qv->size() ? (*qv)[k] : 0);
+            o << "}";
+        }
+        o << "};\n";
+    }
+    return groups;
+}
+
 // Source of the warp-sliced forward (mode 0: pk_fwd over FwdArgs), serving-
 // pool (mode 1: pk_pool over PoolArgs) or exact-adjoint (mode 2: pk_adj over
 // AdjArgs) kernel.
@@ -619,7 +754,16 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
       << " P=" << pat.P() << " slices=" << sl.L << " published=" << sl.NP << " rolled=" << (roll ? 1 : 0) << "\n";
     o << "#include \"rk4_core.cuh\"\nnamespace pk {\n";
     o << "typedef " << (key.f32 ? "float" : "double") << " R;\n";
+    // Each slice's struct is first written with its slice-dependent indices as
+    // hooks (share_slices): component indices (N), published offsets (P),
+    // value indices (Q), offsets of the compensated gradient totals (G) and
+    // ranks of the max-tracked components (R).
+    std::vector<std::string> slice_src(sl.L);
+    long long pk_off = 0;   // gradient totals: slice after slice, 64 floats per value
+    auto H = [](char kind, long long v) { return std::string(1, '\x01') + kind + std::to_string(v) + '\x02'; };
     for (int w = 0; w < sl.L; ++w) {
+        std::ostringstream slice_text;
+        std::ostringstream& o = slice_text;
         const std::vector<int>& own = sl.own[w];
         const int MM = (int)own.size();
         auto mine = [&](int j) { return sl.owner[j] == w; };
@@ -673,12 +817,19 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             std::sort(v->begin(), v->end());
             v->erase(std::unique(v->begin(), v->end()), v->end());
         }
-        std::sort(pown.begin(), pown.end());
-        std::map<int, int> pslot;
+        std::map<int, int> pslot;   // in the order the terms are visited
         for (int q : pown) pslot[q] = (int)pslot.size();
+        std::vector<int> pq(pslot.size());
+        for (auto& kv : pslot) pq[kv.second] = kv.first;
+        // local names of the foreign operands: the same text for slices that are
+        // translates of each other
+        std::map<int, int> fx, fy, fw;
+        for (int j : foreign) fx[j] = (int)fx.size();
+        for (int j : yforeign) fy[j] = (int)fy.size();
+        for (int i : wforeign) fw[i] = (int)fw.size();
         auto val = [&](int q) { return slot.count(q) ? "p[" + S(slot[q]) + "]" : hexlit(lit.value[q]); };
-        auto x = [&](int j) { return mine(j) ? "X[" + S(sl.local[j]) + "]" : "x" + S(j); };
-        o << "struct SL" << w << " {\n";
+        auto x = [&](int j) { return mine(j) ? "X[" + S(sl.local[j]) + "]" : "x" + S(fx.at(j)); };
+        o << "struct \x03 {\n\x04";
         o << "  static constexpr int MM = " << MM << ", NP = " << sl.NP << ", PO = " << std::max<size_t>(pown.size(), 1)
           << ";\n";
         o << "  static constexpr bool FORCED = " << (forced ? "true" : "false")
@@ -687,26 +838,32 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
         o << "  R p[" << std::max<size_t>(slot.size(), 1) << "];\n";
         if (key.ext) o << "  R q[" << std::max<size_t>(slot_lo.size(), 1) << "];   // low parts of the values\n";
         o << "  __device__ __forceinline__ void load(const R* __restrict__ vals, long long B, int b) {\n";
-        for (auto& kv : slot) o << "    p[" << kv.second << "] = vals[" << kv.first << "LL * B + b];\n";
-        for (auto& kv : slot_lo)
-            o << "    q[" << kv.second << "] = vals[" << (pat.P() + kv.first) << "LL * B + b];\n";
+        {
+            std::vector<int> qs(slot.size()), ql(slot_lo.size());
+            for (auto& kv : slot) qs[kv.second] = kv.first;
+            for (auto& kv : slot_lo) ql[kv.second] = kv.first;
+            for (size_t k = 0; k < qs.size(); ++k)
+                o << "    p[" << k << "] = vals[(long long)" << H('Q', qs[k]) << " * B + b];\n";
+            for (size_t k = 0; k < ql.size(); ++k)
+                o << "    q[" << k << "] = vals[(long long)" << H('Q', pat.P() + ql[k]) << " * B + b];\n";
+        }
         o << "  }\n";
         o << "  template <class V> __device__ __forceinline__ void load_vec(V& X, const R* __restrict__ src, long long B,"
              " int b) const {\n";
-        for (int k = 0; k < MM; ++k) o << "    X[" << k << "] = src[" << own[k] << "LL * B + b];\n";
+        for (int k = 0; k < MM; ++k) o << "    X[" << k << "] = src[(long long)" << H('N', own[k]) << " * B + b];\n";
         o << "  }\n";
         o << "  __device__ __forceinline__ void prefetch_vec(const R* src, long long B, int b) const {\n";
-        for (int k = 0; k < MM; ++k) o << "    pk_prefetch_l2(src + " << own[k] << "LL * B + b);\n";
+        for (int k = 0; k < MM; ++k) o << "    pk_prefetch_l2(src + (long long)" << H('N', own[k]) << " * B + b);\n";
         o << "  }\n";
         o << "  template <class V> __device__ __forceinline__ void store_vec(const V& X, R* dst, long long B, int b)"
              " const {\n";
-        for (int k = 0; k < MM; ++k) o << "    dst[" << own[k] << "LL * B + b] = X[" << k << "];\n";
+        for (int k = 0; k < MM; ++k) o << "    dst[(long long)" << H('N', own[k]) << " * B + b] = X[" << k << "];\n";
         o << "  }\n";
         o << "  template <class V> __device__ __forceinline__ void store_traj(const V& X, R* dst, long long B, int b)"
              " const { store_vec(X, dst, B, b); }\n";
         o << "  template <class V> __device__ __forceinline__ void publish(const V& X, R* buf) const {\n";
         for (int k = 0; k < MM; ++k)
-            if (sl.pub[own[k]] >= 0) o << "    buf[" << sl.pub[own[k]] * 32 << "] = X[" << k << "];\n";
+            if (sl.pub[own[k]] >= 0) o << "    buf[" << H('P', sl.pub[own[k]] * 32) << "] = X[" << k << "];\n";
         o << "  }\n";
         o << "  template <class V> __device__ __forceinline__ void track_max(const V& X, V& Mx) const {\n";
         for (int k = 0; k < MM; ++k)
@@ -719,7 +876,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             int rank = 0;
             for (int i = 0; i < n && i < 64; ++i)
                 if ((key.max_mask >> i) & 1ull) {
-                    if (sl.owner[i] == w) o << "    out[" << rank << "LL * B + b] = Mx[" << sl.local[i] << "];\n";
+                    if (sl.owner[i] == w) o << "    out[(long long)" << H('R', rank) << " * B + b] = Mx[" << sl.local[i] << "];\n";
                     ++rank;
                 }
         }
@@ -730,7 +887,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             o << "    typedef M<R> m;\n";
             for (int i = 0; i < n && i < 64; ++i)
                 if ((key.sq_mask >> i) & 1ull) {
-                    const std::string q = sl.owner[i] == w ? "X[" + S(sl.local[i]) + "]" : "buf[" + S(sl.pub[i] * 32) + "]";
+                    const std::string q = sl.owner[i] == w ? "X[" + S(sl.local[i]) + "]" : "buf[" + H('P', sl.pub[i] * 32) + "]";
                     o << "    { const R q = " << q << ";\n";
                     o << "      if (KAHAN) { const R y = m::sub(m::mul(q, q), sqc); const R t = m::add(sq, y);"
                          " sqc = m::sub(m::sub(t, sq), y); sq = t; } else { sq = m::fma(q, q, sq); } }\n";
@@ -740,7 +897,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
         o << "  template <class V, class F> __device__ __forceinline__ void rhs(const V& X, const R* buf, R u, F& f)"
              " const {\n";
         o << "    typedef M<R> m;\n    R a, c;\n";
-        for (int j : foreign) o << "    const R x" << j << " = buf[" << sl.pub[j] * 32 << "];\n";
+        for (int j : foreign) o << "    const R x" << fx.at(j) << " = buf[" << H('P', sl.pub[j] * 32) << "];\n";
         for (int k = 0; k < MM; ++k) {
             const int i = own[k];
             const std::vector<Term>& ts = dt[i];
@@ -778,7 +935,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
                             if (!mine(t.ops[k])) used.push_back(t.ops[k]);
             std::sort(used.begin(), used.end());
             used.erase(std::unique(used.begin(), used.end()), used.end());
-            for (int j : used) o << "    const R x" << j << " = buf[" << sl.pub[j] * 32 << "];\n";
+            for (int j : used) o << "    const R x" << fx.at(j) << " = buf[" << H('P', sl.pub[j] * 32) << "];\n";
             for (int k = 0; k < MM; ++k) {
                 int cnt = 0;
                 for (const Term& t : dt[own[k]]) {
@@ -802,14 +959,14 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             o << "    (void)u;\n  }\n";
         }
         if (adj) {
-            auto W = [&](int i) { return mine(i) ? "W[" + S(sl.local[i]) + "]" : "w" + S(i); };
-            auto Y = [&](int j) { return mine(j) ? "Y[" + S(sl.local[j]) + "]" : "y" + S(j); };
+            auto W = [&](int i) { return mine(i) ? "W[" + S(sl.local[i]) + "]" : "w" + S(fw.at(i)); };
+            auto Y = [&](int j) { return mine(j) ? "Y[" + S(sl.local[j]) + "]" : "y" + S(fy.at(j)); };
             auto out = [&](int j) { return "out[" + S(sl.local[j]) + "]"; };
             o << "  template <class V, class PA> __device__ __forceinline__ void vjp(const V& Y, const R* yb, const V& W,"
                  " const R* wb, R u, V& out, PA& pacc) const {\n";
             o << "    typedef M<R> m;\n";
-            for (int j : yforeign) o << "    const R y" << j << " = yb[" << sl.pub[j] * 32 << "];\n";
-            for (int i : wforeign) o << "    const R w" << i << " = wb[" << sl.pub[i] * 32 << "];\n";
+            for (int j : yforeign) o << "    const R y" << fy.at(j) << " = yb[" << H('P', sl.pub[j] * 32) << "];\n";
+            for (int i : wforeign) o << "    const R w" << fw.at(i) << " = wb[" << H('P', sl.pub[i] * 32) << "];\n";
             for (int k = 0; k < MM; ++k) o << "    out[" << k << "] = R(0);\n";
             for (const auto& it : scatter) {
                 const int i = it.first;
@@ -853,8 +1010,8 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
                 o << "  template <class V> __device__ __forceinline__ void vjp_lo(const V& Y, const R* yb, const V& W,"
                      " const R* wb, R u, V& out) const {\n";
                 o << "    typedef M<R> m;\n";
-                for (int j : yforeign) o << "    const R y" << j << " = yb[" << sl.pub[j] * 32 << "];\n";
-                for (int i : wforeign) o << "    const R w" << i << " = wb[" << sl.pub[i] * 32 << "];\n";
+                for (int j : yforeign) o << "    const R y" << fy.at(j) << " = yb[" << H('P', sl.pub[j] * 32) << "];\n";
+                for (int i : wforeign) o << "    const R w" << fw.at(i) << " = wb[" << H('P', sl.pub[i] * 32) << "];\n";
                 for (int k = 0; k < MM; ++k) o << "    out[" << k << "] = R(0);\n";
                 for (const auto& it : scatter) {
                     const int i = it.first;
@@ -895,38 +1052,43 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             o << "  }\n";
             o << "  template <class PV> __device__ __forceinline__ void store_pbar(const PV& PB, double* pbar, long long B,"
                  " int b) const {\n";
-            for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = PB[" << kv.second << "];\n";
+            for (size_t k = 0; k < pq.size(); ++k) o << "    pbar[(long long)" << H('Q', pq[k]) << " * B + b] = PB[" << k << "];\n";
             o << "  }\n";
             o << "  template <class PV> __device__ __forceinline__ void load_pbar(PV& PB, const double* pbar, long long B,"
                  " int b) const {\n";
-            for (auto& kv : pslot) o << "    PB[" << kv.second << "] = pbar[" << kv.first << "LL * B + b];\n";
+            for (size_t k = 0; k < pq.size(); ++k) o << "    PB[" << k << "] = pbar[(long long)" << H('Q', pq[k]) << " * B + b];\n";
             o << "  }\n";
             o << "  __device__ __forceinline__ void zero_pbar(double* pbar, long long B, int b) const {\n";
-            for (auto& kv : pslot) o << "    pbar[" << kv.first << "LL * B + b] = 0.0;\n";
+            for (size_t k = 0; k < pq.size(); ++k) o << "    pbar[(long long)" << H('Q', pq[k]) << " * B + b] = 0.0;\n";
             o << "  }\n";
-            // FP32 compensated per-chunk totals in shared memory: value q's sum
-            // at pk[64 q], its compensation at pk[64 q + 32] (pk holds the lane)
+            // FP32 compensated per-chunk totals in shared memory, slice after
+            // slice: the k-th value's sum at pk[64 (off + k)], its compensation
+            // 32 floats further (pk holds the lane)
+            auto PS = [&](size_t k) { return H('G', 64 * (pk_off + (long long)k)); };
+            auto PC = [&](size_t k) { return H('G', 64 * (pk_off + (long long)k) + 32); };
             o << "  template <class PV> __device__ __forceinline__ void add_pk(const PV& ps, R* pk) const {\n";
-            for (auto& kv : pslot)
-                o << "    { R s_ = pk[" << 64 * kv.first << "], c_ = pk[" << 64 * kv.first + 32
-                  << "]; kahan_add(s_, c_, ps[" << kv.second << "]); pk[" << 64 * kv.first << "] = s_; pk["
-                  << 64 * kv.first + 32 << "] = c_; }\n";
+            for (size_t k = 0; k < pq.size(); ++k)
+                o << "    { R s_ = pk[" << PS(k) << "], c_ = pk[" << PC(k) << "]; kahan_add(s_, c_, ps[" << k
+                  << "]); pk[" << PS(k) << "] = s_; pk[" << PC(k) << "] = c_; }\n";
             o << "  }\n";
             o << "  template <bool EXT> __device__ __forceinline__ void flush_pk(R* pk, double* pbar, long long B,"
                  " int b, double s) const {\n";
-            for (auto& kv : pslot)
-                o << "    { const double t_ = (double)pk[" << 64 * kv.first << "] - (double)pk[" << 64 * kv.first + 32
-                  << "]; pbar[" << kv.first << "LL * B + b] = EXT ? M<double>::fma(s, t_, pbar[" << kv.first
-                  << "LL * B + b]) : pbar[" << kv.first << "LL * B + b] + t_; pk[" << 64 * kv.first << "] = R(0); pk["
-                  << 64 * kv.first + 32 << "] = R(0); }\n";
+            for (size_t k = 0; k < pq.size(); ++k) {
+                const std::string pb = "pbar[(long long)" + H('Q', pq[k]) + " * B + b]";
+                o << "    { const double t_ = (double)pk[" << PS(k) << "] - (double)pk[" << PC(k) << "]; " << pb
+                  << " = EXT ? M<double>::fma(s, t_, " << pb << ") : " << pb << " + t_; pk[" << PS(k)
+                  << "] = R(0); pk[" << PC(k) << "] = R(0); }\n";
+            }
             o << "  }\n";
             o << "  __device__ __forceinline__ void zero_pk(R* pk) const {\n";
-            for (auto& kv : pslot)
-                o << "    pk[" << 64 * kv.first << "] = R(0); pk[" << 64 * kv.first + 32 << "] = R(0);\n";
+            for (size_t k = 0; k < pq.size(); ++k) o << "    pk[" << PS(k) << "] = R(0); pk[" << PC(k) << "] = R(0);\n";
             o << "  }\n";
         }
         o << "};\n";
+        slice_src[w] = slice_text.str();
+        pk_off += (long long)pq.size();
     }
+    const std::vector<SliceGroup> groups = share_slices(slice_src, o);
     o << "}  // namespace pk\n";
     const std::string ext = key.ext ? "true" : "false";
     const std::string kahan = key.kahan ? "true" : "false", hmax = key.max_mask ? "true" : "false",
@@ -941,18 +1103,25 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
     o << "  const bool valid = bb < cnt;\n";
     o << "  const int b = valid ? (int)bb : (int)cnt - 1;\n";
     o << "  R* sm = reinterpret_cast<R*>(pk_dyn_smem()) + lane;\n";
+    std::ostringstream call;
+    if (mode == 1)
+        call << "ws_pool<R, " << kahan << ", " << hmax << ", " << hsq << ", " << n << ">(sl, p, sm, b, valid, w);";
+    else if (mode == 0)
+        call << "ws_fwd<R, " << kahan << ", " << hmax << ", " << hsq << ", " << htraj << ", " << n << ", " << ext
+             << ">(sl, a, sm, b, valid);";
+    else   // the Kahan mode of the forward passes is the plan's (AdjArgs::kahan)
+        call << "ws_adj<R, " << kahan << ", " << hsq << ", " << (key.f32 ? "true" : "false") << ", " << n << ", " << ext
+             << ">(sl, a, sm, b, valid);";
     o << "  switch (w) {\n";
-    for (int w = 0; w < sl.L; ++w) {
-        o << "    case " << w << ": { SL" << w << " sl; ";
-        if (mode == 1)
-            o << "ws_pool<R, " << kahan << ", " << hmax << ", " << hsq << ", " << n << ">(sl, p, sm, b, valid, w);";
-        else if (mode == 0)
-            o << "ws_fwd<R, " << kahan << ", " << hmax << ", " << hsq << ", " << htraj << ", " << n << ", " << ext
-              << ">(sl, a, sm, b, valid);";
-        else   // the Kahan mode of the forward passes is the plan's (AdjArgs::kahan)
-            o << "ws_adj<R, " << kahan << ", " << hsq << ", " << (key.f32 ? "true" : "false") << ", " << n << ", "
-              << ext << ">(sl, a, sm, b, valid);";
-        o << " } break;\n";
+    for (const SliceGroup& g : groups) {
+        const std::string name = "SL" + std::to_string(g.ref);
+        o << "   ";
+        for (int m : g.members) o << " case " << m << ":";
+        o << " { " << name << " sl; ";
+        if (g.members.size() > 1)
+            o << "sl.nb_ = " << name << "_NB[w]; sl.pb_ = " << name << "_PGR[w][0]; sl.gb_ = " << name
+              << "_PGR[w][1]; sl.rb_ = " << name << "_PGR[w][2]; sl.qt_ = " << name << "_QT[w]; ";
+        o << call.str() << " } break;\n";
     }
     o << "    default: break;\n  }\n}\n";
     // FP32 adjoint with a slice holding more than 16 values: their compensated
@@ -966,7 +1135,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
             max_po = std::max(max_po, po);
         }
     }
-    const long long pk_floats = max_po > 16 ? 64LL * pat.P() : 0;
+    const long long pk_floats = max_po > 16 ? 64LL * std::max<long long>(pat.P(), pk_off) : 0;
     o << "// ws-launch " << 32 * sl.L << " " << ((adj ? 6 : 2) * sl.NP * 32 + pk_floats) * (key.f32 ? 4 : 8)
       << "\n";
     return o.str();

@@ -719,7 +719,10 @@ std::vector<SliceGroup> share_slices(const std::vector<std::string>& src, std::o
 // Source of the warp-sliced forward (mode 0: pk_fwd over FwdArgs), serving-
 // pool (mode 1: pk_pool over PoolArgs) or exact-adjoint (mode 2: pk_adj over
 // AdjArgs) kernel.
-std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, int mode) {
+// roll_force: -1 = the rule below, 0 / 1 = unrolled / rolled stages.
+// *distinct: number of distinct slice structs after share_slices.
+std::string ws_source_impl(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, int mode, int roll_force,
+                           int* distinct) {
     const int n = pat.n;
     const bool adj = mode == 2;
     const auto dt = dest_terms(pat);
@@ -746,6 +749,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
     // and the 64-state banded system 1.0-1.5x faster rolled, 128-state chain 1.35x
     // faster unrolled.
     bool roll = adj ? (n > 24 && n <= 96) : (double)terms / sl.L >= 30.0;
+    if (roll_force >= 0) roll = roll_force != 0;
     if (const char* e = std::getenv("PASIF_WS_ROLL")) roll = std::atoi(e) != 0;   // tuning override
     std::ostringstream o;
     o << "// generated by pasif_gb300 jit.cpp: warp-sliced "
@@ -1089,6 +1093,7 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
         pk_off += (long long)pq.size();
     }
     const std::vector<SliceGroup> groups = share_slices(slice_src, o);
+    if (distinct) *distinct = (int)groups.size();
     o << "}  // namespace pk\n";
     const std::string ext = key.ext ? "true" : "false";
     const std::string kahan = key.kahan ? "true" : "false", hmax = key.max_mask ? "true" : "false",
@@ -1139,6 +1144,32 @@ std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKe
     o << "// ws-launch " << 32 * sl.L << " " << ((adj ? 6 : 2) * sl.NP * 32 + pk_floats) * (key.f32 ? 4 : 8)
       << "\n";
     return o.str();
+}
+
+// Warp-sliced kernel source.  Where most slices share one struct
+// (share_slices) the stages are unrolled: with the warps of a block running
+// the same code the instruction cache holds it (GB300, FP32-Kahan, 4096
+// systems: 32-DOF chain adjoint, 16 warps, 1.0e9 adjoint system-steps/s
+// unrolled vs 7.9e8 rolled; 16-DOF chain adjoint, 8 warps, 1.89e9 vs 1.46e9).
+std::string ws_source(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, int mode) {
+    int distinct = 0;
+    std::string src = ws_source_impl(pat, lit, key, mode, -1, &distinct);
+    const bool rolled = src.find(" rolled=1") != std::string::npos;
+    if (rolled && 2 * distinct <= key.slices && !std::getenv("PASIF_WS_ROLL"))
+        src = ws_source_impl(pat, lit, key, mode, 0, &distinct);
+    return src;
+}
+
+// Whether the slices of `pat` cut into L warps are translates of one
+// another for the most part (at most L/2 distinct structs).
+bool ws_shareable(const Pattern& pat, int L, bool adjoint) {
+    FwdKernelKey key;
+    key.f32 = true;
+    key.kahan = true;
+    key.slices = L;
+    int distinct = 0;
+    ws_source_impl(pat, Literals(), key, adjoint ? 2 : 0, 0, &distinct);
+    return 2 * distinct <= L;
 }
 
 // Launch shape recorded by ws_source on its last line.
@@ -1563,6 +1594,50 @@ bool get_fwd_kernel(const Pattern& pat, const Literals& lit, const FwdKernelKey&
     return get_cached(fwd_source(pat, lit, key), "pk_fwd", key.block, out, err);
 }
 
+namespace {
+// FP32 slices that share their code (ws_shareable) are cut finer: more warps
+// per system, the same instructions for most of them.  GB300, FP32-Kahan,
+// 4096 systems, default -> finer slices: forward 64-DOF chain (128 states) 4
+// -> 16 warps 2.65e9 -> 3.68e9 system-steps/s, 32-DOF chain 4 -> 8 warps
+// 4.0e9 -> 5.5e9; adjoint 64-DOF chain 8 -> 16 warps 3.6e8 -> 4.5e8 adjoint
+// system-steps/s, 32-DOF chain 6 -> 16 warps 4.7e8 -> 1.0e9, 16-DOF chain 4
+// -> 8 warps 1.45e9 -> 1.89e9.  So: 8 states per warp forward, 4 adjoint, at
+// most 16 warps, where that cut shares.  Patterns whose slices differ (the
+// banded system with random cubic entries) keep the register-bound split.
+int ws_more_if_shared(const Pattern& pat, int L, bool allowed, bool adjoint) {
+    if (!allowed || std::getenv("PASIF_WS_SLICES") || std::getenv(adjoint ? "PASIF_WS_SLICES_ADJ" : "PASIF_WS_SLICES_FWD"))
+        return L;
+    const int L2 = std::min(16, pat.n / (adjoint ? 4 : 8));
+    if (L2 <= L) return L;
+    // memoised per pattern: the check generates the kernel source
+    static std::mutex mu;
+    static std::map<std::string, bool> memo;
+    std::ostringstream k;
+    k << pat.n << (adjoint ? 'a' : 'f') << L2 << ':';
+    for (int v : pat.k_ptr) k << v << ',';
+    k << ';';
+    for (int v : pat.k_col) k << v << ',';
+    k << ';';
+    for (int v : pat.g_idx) k << v << ',';
+    k << ';';
+    for (int v : pat.l_idx) k << v << ',';
+    k << ';';
+    for (int v : pat.p_idx) k << v << ',';
+    k << ';';
+    for (int v : pat.f_idx) k << v << ',';
+    const std::string key = k.str();
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = memo.find(key);
+        if (it != memo.end()) return it->second ? L2 : L;
+    }
+    const bool ok = ws_shareable(pat, L2, adjoint);
+    std::lock_guard<std::mutex> g(mu);
+    memo[key] = ok;
+    return ok ? L2 : L;
+}
+}  // namespace
+
 int ws_slices(const Pattern& pat, bool f32, bool force, int B, bool ext) {
     const int n = pat.n;
     // Measured crossovers on GB300 (time sliced / thread per system, 4096 systems):
@@ -1575,7 +1650,7 @@ int ws_slices(const Pattern& pat, bool f32, bool force, int B, bool ext) {
         const bool small_batch = B > 0 && B <= 8192;
         if (f32 ? n < 28 : (n < 3 || (n < 8 && !small_batch))) return 0;
     }
-    return ws_split(n, f32, force, false, ext);
+    return ws_more_if_shared(pat, ws_split(n, f32, force, false, ext), f32 && !force && !ext, false);
 }
 
 int ws_slices_adjoint(const Pattern& pat, bool f32, bool force, bool ext) {
@@ -1585,7 +1660,7 @@ int ws_slices_adjoint(const Pattern& pat, bool f32, bool force, bool ext) {
     // states 0.75, 8 states 0.62, 4 states 0.93, 2 states 1.12; FP64 2 states
     // 0.68, 4-8 states 0.33-0.44.
     if (n < 2 || n > kWsMaxN || (!force && f32 && n < 5)) return 0;
-    return ws_split(n, f32, force, true, ext);
+    return ws_more_if_shared(pat, ws_split(n, f32, force, true, ext), f32 && !force && !ext, true);
 }
 
 int ws_split(int n, bool f32, bool force, bool adjoint, bool ext) {

@@ -344,6 +344,64 @@ def test_generated_adjoint_banded32_default_slices(tmp_path):
     assert np.abs(out[0][0]).max() > 0
 
 
+def _distinct_structs(src):
+    return len(re.findall(r"^struct SL\d+ \{", src, flags=re.M))
+
+
+@pytest.mark.parametrize("prec", ["fp32_kahan", "fp64"])
+def test_shared_slices_chain_forward(tmp_path, prec):
+    """32-DOF spring chain (64 states), default warp-sliced kernels: the
+    interior slices are translates of one another and share one struct
+    (runtime bases, per-warp value table); FP32 cuts the chain into 8 warps.
+    Equal to the oracle."""
+    w = synth.chain8(n_sys=5, nsteps=120, nd=32)
+    src = Plan(w.pattern, prec).jit_report(w.values, window=w.window, im=w.im)
+    src = src.split("// ---- source ----\n", 1)[1]
+    L = int(re.search(r"slices=(\d+)", src).group(1))
+    if prec == "fp32_kahan":
+        assert L == 8
+        assert 2 * _distinct_structs(src) <= L, (_distinct_structs(src), L)
+    got = run_emulated(tmp_path, w.pattern, w.values, w.x0, w.exc_index, w.signals, w.window, w.im, w.h, 0,
+                       w.nsteps, prec)
+    ref, _, _ = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
+                                prec)
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_shared_slices_chain_adjoint(tmp_path):
+    """16-DOF spring chain (32 states), FP32-Kahan: the default adjoint cuts
+    it into 8 warps whose interior slices share one struct; it gives the bits
+    of the thread-per-system adjoint.  FP64, forced 16-warp split (shared
+    structs too): the oracle's exact adjoint bit for bit."""
+    w = synth.chain8(n_sys=4, nsteps=40, nd=16)
+    rng = np.random.default_rng(41)
+    gf = rng.normal(size=(w.n_sys, w.pattern.n))
+    gs = rng.normal(size=w.n_sys)
+    sq, N = (0, 3), 40
+    mask = (1 << 0) | (1 << 3)
+    rep = Plan(w.pattern, "fp32_kahan").jit_report_adjoint(w.values, sq_mask=mask).split("// ---- source ----\n", 1)[1]
+    assert "slices=8 " in rep.splitlines()[0]
+    assert 2 * _distinct_structs(rep) <= 8
+    out = []
+    for slicing in (None, False):
+        d = os.path.join(str(tmp_path), str(slicing))
+        os.makedirs(d)
+        out.append(run_emulated_adjoint(d, w.pattern, "fp32_kahan", slicing, w.values, w.x0, w.exc_index, w.signals,
+                                        np.asarray(w.im), gf, gs, N, sq, N // 3, h=w.h))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    rep64 = Plan(w.pattern, "fp64", slicing=True).jit_report_adjoint(w.values, sq_mask=mask)
+    assert 2 * _distinct_structs(rep64.split("// ---- source ----\n", 1)[1]) <= 16
+    d = os.path.join(str(tmp_path), "fp64")
+    os.makedirs(d)
+    dv, dx = run_emulated_adjoint(d, w.pattern, "fp64", True, w.values, w.x0, w.exc_index, w.signals,
+                                  np.asarray(w.im), gf, gs, N, sq, N // 3, h=w.h)
+    odv, odx = O.batch_adjoint(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, N, w.window, w.im, gf, gs, sq,
+                               N // 3)
+    np.testing.assert_array_equal(dv, odv)
+    np.testing.assert_array_equal(dx, odx)
+
+
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan", "fp32_ext"])
 @pytest.mark.parametrize("slicing", [False, True])
 @pytest.mark.parametrize("split", [1, 2])

@@ -1219,7 +1219,7 @@ void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em,
 // compensated forwards are packed only for n <= 6 with a destination pair of
 // at least 4 terms on each side.  PASIF_FP32X2 overrides the choice (tuning).
 int fwd_paired(const Pattern& pat, const FwdKernelKey& key) {
-    if (!key.f32 || key.ext || key.fast || key.slices >= 2) return 0;
+    if (!key.f32 || key.fast || key.slices >= 2) return 0;
     std::vector<int> cnt(pat.n, 0);
     for (int i = 0; i < pat.n; ++i) cnt[i] = pat.k_ptr[i + 1] - pat.k_ptr[i];
     for (int e = 0; e < pat.g_nnz(); ++e) ++cnt[pat.g_idx[3 * e]];
@@ -1231,7 +1231,7 @@ int fwd_paired(const Pattern& pat, const FwdKernelKey& key) {
         dense += cnt[i] >= 4 && cnt[i + 1] >= 4;
     }
     if (both == 0) return 0;
-    int mode = !key.kahan ? 2 : (pat.n <= 6 && dense > 0) ? 2 : 0;
+    int mode = (!key.kahan && !key.ext) ? 2 : (pat.n <= 6 && dense > 0) ? (key.ext ? 1 : 2) : 0;
     if (const char* e = std::getenv("PASIF_FP32X2")) mode = std::max(0, std::min(2, std::atoi(e)));
     return mode;
 }

@@ -365,7 +365,8 @@ __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K
     typedef M<R> m;
     static_assert(!EXT || N > 0, "extended-state steps need a compile-time state size");
     static_assert(!FAST || (!EXT && NSTG == 0), "fast steps are plain forward steps");
-    static_assert(!PAIR || (sizeof(R) == 4 && N > 0 && !EXT && !FAST && NSTG <= 1), "paired steps: FP32 forward");
+    static_assert(!PAIR || (sizeof(R) == 4 && N > 0 && !FAST && NSTG <= 1 && (!EXT || PAIR == 1)),
+                  "paired steps: FP32 forward; extended state with the scalar update");
     const int n = N ? N : sys.dim();
     if constexpr (PAIR) {
         typedef M2 p2;
@@ -375,6 +376,8 @@ __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K
 #pragma unroll
             for (int i = 0; i < N; ++i) stg[i * sB] = Q[i];
         }
+        RegVec<R, EXT ? N : 1> Kc;
+        if constexpr (EXT) sys.template rhs_lo<true>(Q, Q, ua, Kc);
         sys.template rhs<true>(Q, Q, ua, K);
 #pragma unroll
         for (int i = 0; i + 1 < N; i += 2) {
@@ -405,6 +408,11 @@ __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K
             }
         }
         sys.template rhs<true>(Mi, Mi, uc, K);
+        if constexpr (EXT) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) ext_update(Q[i], Cm[i], m::add(S[i], K[i]), Kc[i], h, h6, h6lo);
+            return;
+        }
         if constexpr (KAHAN && PAIR == 1) {
 #pragma unroll
             for (int i = 0; i < N; ++i) {
@@ -648,7 +656,8 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     typedef M<R> m;
     constexpr int W = WP::W;
     constexpr bool FASTK = WP::FAST && HTRAJ == 0 && !EXT;   // fast steps: plain forwards only
-    constexpr int PAIRK = (WP::PAIR && !EXT && !FASTK) ? WP::PAIR : 0;   // paired (f32x2) steps: FP32 forwards
+    // paired (f32x2) steps: FP32 forwards (extended state: packed stages only)
+    constexpr int PAIRK = (WP::PAIR && !FASTK) ? (EXT ? 1 : WP::PAIR) : 0;
     constexpr unsigned SPI = W == 0 ? 1u : (unsigned)(W / 2);
     constexpr int STG = HTRAJ == 2 ? adj_slot_vecs<R>() : 0;
     const long long B = a.B;

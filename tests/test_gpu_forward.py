@@ -50,11 +50,12 @@ def test_forward_bit_exact_random_patterns(gpu, prec, generic, seed):
 
 
 @pytest.mark.parametrize("mode", [1, 2])
-@pytest.mark.parametrize("prec", ["fp32", "fp32_kahan"])
+@pytest.mark.parametrize("prec", ["fp32", "fp32_kahan", "fp32_ext"])
 @pytest.mark.parametrize("seed", range(4))
 def test_packed_fp32_forward_bit_exact(gpu, monkeypatch, mode, prec, seed):
     """Packed-FP32 (f32x2) forward kernels forced on random patterns (mode 1:
-    packed stages, scalar compensated update; 2: packed update too), K values
+    packed stages, scalar compensated update; 2: packed update too; the
+    extended-state update is always scalar), K values
     of exactly 1 and -1 folded as literals, reducers on: equal to the oracle
     bit for bit (ptxas must not contract a packed product into an add)."""
     monkeypatch.setenv("PASIF_FP32X2", str(mode))

@@ -98,12 +98,13 @@ def test_generated_kernel_matches_oracle(tmp_path, prec, seed, W, step0, nsteps,
 
 
 @pytest.mark.parametrize("mode", [1, 2])
-@pytest.mark.parametrize("prec", ["fp32", "fp32_kahan"])
+@pytest.mark.parametrize("prec", ["fp32", "fp32_kahan", "fp32_ext"])
 @pytest.mark.parametrize("seed", range(3))
 def test_packed_fp32_kernel_matches_oracle(tmp_path, monkeypatch, mode, prec, seed):
     """Packed-FP32 (f32x2) forward, forced on random patterns (mode 1:
-    packed stages and scalar compensated update, 2: packed update too), with
-    K values of exactly 1 and -1 folded as literals: the oracle's bits."""
+    packed stages and scalar compensated update, 2: packed update too; the
+    extended-state update is always scalar), with K values of exactly 1 and
+    -1 folded as literals: the oracle's bits."""
     monkeypatch.setenv("PASIF_FP32X2", str(mode))
     rng = np.random.default_rng(900 + seed)
     pat, v = cases.random_system(rng, n=[2, 5, 6][seed])

@@ -401,6 +401,7 @@ def main():
         return wl.n_sys * wl.nsteps / (f0.elapsed_time(f1) * 1e-3), mx, bt.kernel_info()
 
     other = {}
+
     def amp_err(m, ref):
         # per-system relative amplitude error over the systems finite in both
         fin = np.isfinite(m).all(axis=1) & np.isfinite(ref).all(axis=1)
@@ -427,6 +428,9 @@ def main():
                        "speedup_fp32_kahan": r32 / r64,
                        "flops_per_system_step": wl.flops_per_system_step(),
                        "fp32_kahan_tflops": r32 * wl.flops_per_system_step() / 1e12,
+                       # fractions of the FMA peaks measured in this run (algorithmic FLOPs)
+                       "fp32_kahan_frac_of_fp32_peak": r32 * wl.flops_per_system_step() / (peak.value * 1e12),
+                       "fp64_frac_of_fp64_peak": r64 * wl.flops_per_system_step() / (peak64.value * 1e12),
                        "amplitude_rel_err_fp32_kahan_vs_fp64": amp_err(m32, m64)}
         if name == "config4_banded32":   # the precision study: plain FP32 and the extended-state mode as well
             rp, mp, _ = timed_forward(wl, "fp32")

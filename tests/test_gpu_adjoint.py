@@ -254,3 +254,28 @@ def test_adjoint_banded32_default_slices(gpu, storage):
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
     assert np.isfinite(out[0][0]).all() and np.abs(out[0][0]).max() > 0
+
+
+@pytest.mark.parametrize("nd,n_sys", [(32, 300), (64, 100)])
+def test_shared_slice_code_same_bits(gpu, monkeypatch, nd, n_sys):
+    """Spring chains of 32 and 64 DOF (64, 128 states): the default kernels,
+    whose interior warp slices share one struct (finer cut: 8 / 16 warps),
+    give the bits of kernels with one struct per warp, forward (states and
+    running max) and FP32-Kahan adjoint (stored trajectory and checkpoints)."""
+    w = synth.chain8(n_sys=n_sys, nsteps=602, nd=nd)
+    comps = tuple(range(nd))
+    out = {}
+    for share in ("1", "0"):
+        monkeypatch.setenv("PASIF_WS_SHARE", share)
+        plan = Plan(w.pattern, "fp32_kahan")
+        sig = Signals(w.signals, w.window, w.im, "fp32_kahan")
+        b = Batch(plan, w.values, w.x0, w.exc_index)
+        b.forward(sig, w.h, 600, max_comp=comps[:8], max_start=300)
+        res = list(b.get())
+        for storage in (0, 1 << 30):
+            b.adjoint_storage(storage)
+            res += list(b.adjoint(sig, w.h, 600, g_sq=np.ones(n_sys), sq_comp=comps, sq_start=300))
+        assert b.kernel_info()["adjoint"] == "specialised"
+        out[share] = res
+    for a, c in zip(out["1"], out["0"]):
+        np.testing.assert_array_equal(a, c)

@@ -429,8 +429,8 @@ def main():
                        "flops_per_system_step": wl.flops_per_system_step(),
                        "fp32_kahan_tflops": r32 * wl.flops_per_system_step() / 1e12,
                        # fractions of the FMA peaks measured in this run (algorithmic FLOPs)
-                       "fp32_kahan_frac_of_fp32_peak": r32 * wl.flops_per_system_step() / (peak.value * 1e12),
-                       "fp64_frac_of_fp64_peak": r64 * wl.flops_per_system_step() / (peak64.value * 1e12),
+                       "fp32_kahan_frac_of_fp32_peak": r32 * wl.flops_per_system_step() / peak.value,
+                       "fp64_frac_of_fp64_peak": r64 * wl.flops_per_system_step() / peak64.value,
                        "amplitude_rel_err_fp32_kahan_vs_fp64": amp_err(m32, m64)}
         if name == "config4_banded32":   # the precision study: plain FP32 and the extended-state mode as well
             rp, mp, _ = timed_forward(wl, "fp32")

@@ -1539,14 +1539,16 @@ std::string pool_source(const Pattern& pat, const FwdKernelKey& key) {
     if (key.slices >= 2) return ws_source(pat, Literals(), key, 1);
     Literals none;   // a pool's slots change owner: every value is loaded
     Emitter em(pat, none);
+    const int pair = fwd_paired(pat, key);   // packed FP32 where the forward kernel packs
     std::ostringstream o;
-    o << "// generated by pasif_gb300 jit.cpp: serving pool chunk, n=" << pat.n << " P=" << pat.P() << "\n";
-    emit_sys_head(o, pat, em, key.f32);
+    o << "// generated by pasif_gb300 jit.cpp: serving pool chunk, n=" << pat.n << " P=" << pat.P()
+      << (pair ? " packed FP32" : "") << "\n";
+    emit_sys_head(o, pat, em, key.f32, false, pair > 0);
     o << "};\n";
     const int W = key.window;
     o << "struct JW {\n  static constexpr int W = " << W << ";\n";
     o << "  static constexpr bool FAST = false;\n";
-    o << "  static constexpr int PAIR = 0;\n";
+    o << "  static constexpr int PAIR = " << pair << ";\n";
     emit_sample_ring(o, W, key.block, pat);
     for (int which = 0; which < 2; ++which) {
         o << "  __device__ static constexpr R " << (which ? "wc" : "wn") << "(int i) { return ";

@@ -252,15 +252,20 @@ def _pool_jobs(rng, pat, v, C, W):
     return jobs
 
 
-@pytest.mark.parametrize("slicing", [False, True])
+@pytest.mark.parametrize("slicing,packed", [(False, False), (True, False), (False, True)])
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan"])
 @pytest.mark.parametrize("seed,W", [(0, 4), (1, 0), (2, 2)])
-def test_generated_pool_matches_oracle(tmp_path, prec, seed, W, slicing):
+def test_generated_pool_matches_oracle(tmp_path, monkeypatch, prec, seed, W, slicing, packed):
     """Serving-pool chunk kernel: every system of every job, run in 16-step
     chunks beside other jobs that join and leave, equals the oracle run of
-    that job alone, bit for bit (state, max and sum-of-squares reducers)."""
+    that job alone, bit for bit (state, max and sum-of-squares reducers);
+    `packed`: the packed-FP32 form forced on."""
     if shutil.which("g++") is None:
         pytest.skip("no host C++ compiler")
+    if packed:
+        if prec == "fp64":
+            pytest.skip("packed FP32 only")
+        monkeypatch.setenv("PASIF_FP32X2", "2")
     rng = np.random.default_rng(900 + seed)
     pat, v = cases.random_system(rng)
     C, chunk = 7, 16
@@ -273,6 +278,8 @@ def test_generated_pool_matches_oracle(tmp_path, prec, seed, W, slicing):
     src = Plan(pat, prec, slicing=slicing).jit_report_pool(W, im, max_comp, sq_comp)
     src = src.split("// ---- source ----\n", 1)[1]
     assert ("warp-sliced" in src) == slicing
+    if packed and pat.n >= 2:
+        assert "packed FP32" in src.splitlines()[0]
     d = str(tmp_path)
     exe, env = build_emulator(d, src, "EMU_POOL")
     dt = np.float64 if prec == "fp64" else np.float32

@@ -225,6 +225,15 @@ int Batch::reserve(int n_sys, int nsteps, std::string* err) {
     return 0;
 }
 
+Batch::~Batch() {
+    for (int i = 0; i < kReplayBufs; ++i) {
+        if (replay_st[i]) cudaStreamDestroy(replay_st[i]);
+        if (ev_replayed[i]) cudaEventDestroy(ev_replayed[i]);
+        if (ev_free[i]) cudaEventDestroy(ev_free[i]);
+    }
+    if (ev_ckpt) cudaEventDestroy(ev_ckpt);
+}
+
 int Batch::resize(int n_sys, std::string* err) {
     if (n_sys < 0) { *err = "negative number of systems"; return 1; }
     B = n_sys;
@@ -602,11 +611,39 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
     const bool replayed = !stored && jit && nsteps > 0 && adj_blocks >= 32 &&
                           fwd_kernel(sig, 0ull, 0ull, 2, &fk, &ferr) && fwd_kernel(sig, 0ull, 0ull, 3, &ckk, &ferr);
     const size_t vec = Bn * (size_t)n * rs;
+    // Replayed: up to kReplayBufs chunk buffers, so that the forward replays
+    // of the next chunks run on their own streams while the backward sweep
+    // works through the current one (the replays are independent: each starts
+    // from its checkpoint).  As many as the buffer already holds (a reserved
+    // batch), or as fit in 256 MiB.
+    const size_t chunk_sz = (slot_vecs() * (size_t)C + 1) * vec;
+    int nbuf = 1;
     if (stored) {
         PK_CUDA(buf.ensure((slot_vecs() * (size_t)nsteps + 1) * vec), "cudaMalloc");
     } else {
         PK_CUDA(ckpt.ensure(Bn * 2 * n * (size_t)(nck > 0 ? nck : 1) * rs), "cudaMalloc");
-        PK_CUDA(buf.ensure((slot_vecs() * (size_t)C + 1) * vec), "cudaMalloc");
+        if (replayed) {
+            const size_t cap = std::max(buf.bytes, std::min((size_t)kReplayBufs * chunk_sz, (size_t)256 << 20));
+            nbuf = (int)std::max<size_t>(1, std::min<size_t>({(size_t)kReplayBufs, cap / chunk_sz, (size_t)nck}));
+        }
+        PK_CUDA(buf.ensure((size_t)nbuf * chunk_sz), "cudaMalloc");
+    }
+    if (nbuf > 1) {   // streams at the priority of st, events (made once per batch)
+        int prio = 0;
+        PK_CUDA(cudaStreamGetPriority(st, &prio), "cudaStreamGetPriority");
+        for (int i = 0; i < nbuf; ++i) {
+            if (replay_st[i] && replay_prio != prio) {
+                PK_CUDA(cudaStreamDestroy(replay_st[i]), "cudaStreamDestroy");
+                replay_st[i] = nullptr;
+            }
+            if (!replay_st[i])
+                PK_CUDA(cudaStreamCreateWithPriority(&replay_st[i], cudaStreamNonBlocking, prio),
+                        "cudaStreamCreateWithPriority");
+            if (!ev_replayed[i]) PK_CUDA(cudaEventCreateWithFlags(&ev_replayed[i], cudaEventDisableTiming), "cudaEventCreate");
+            if (!ev_free[i]) PK_CUDA(cudaEventCreateWithFlags(&ev_free[i], cudaEventDisableTiming), "cudaEventCreate");
+        }
+        replay_prio = prio;
+        if (!ev_ckpt) PK_CUDA(cudaEventCreateWithFlags(&ev_ckpt, cudaEventDisableTiming), "cudaEventCreate");
     }
     if (replayed) PK_CUDA(adj_state.ensure(vec), "cudaMalloc");
     PK_CUDA(pbar.ensure(Bn * (size_t)(P > 0 ? P : 1) * sizeof(double)), "cudaMalloc");
@@ -629,6 +666,7 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
         PK_CUDA(cudaMemcpyAsync(adj_state.p, x0.p, vec, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync");
         PK_CUDA(launch_fwd_jit(ckk, sig, h, 0, nsteps, Reducers(), 0ull, 0ull, C, nck, adj_state.p, ckpt.p, st, x0lo),
                 "checkpoint forward kernel launch");
+        if (nbuf > 1) PK_CUDA(cudaEventRecord(ev_ckpt, st), "cudaEventRecord");
     }
     cudaError_t e;
 #define PK_FILL_ADJ(R_)                                               \
@@ -674,23 +712,49 @@ int Batch::adjoint(const Signals& sig, double h, int nsteps, const Reducers& red
         // Replayed: per chunk, backward order, its slots from its checkpoint then
         // its backward sweep; one chunk at a time keeps the slots in L2 between
         // the two (groups of chunks, 2016 steps for 16 states, ran 3 % slower).
+        // With several chunk buffers, chunk k's replay runs on its buffer's stream
+        // as soon as the checkpoints exist and the backward sweep two or more
+        // chunks back has released that buffer; the sweep of chunk k waits for
+        // its replay (events).  Same kernels on the same data: the same bits.
         if (replayed) {
             const size_t rsz = sizeof(*a.dx0);
+            using RT = typename std::remove_pointer<decltype(a.buf)>::type;
+            RT* const buf0 = a.buf;
             for (int k = nck - 1; k >= 0; --k) {
                 const int t0 = k * C, t1 = std::min(nsteps, t0 + C);
+                const int bi = (nck - 1 - k) % nbuf;
+                char* const bp = static_cast<char*>(buf.p) + (size_t)bi * chunk_sz;
                 const char* ck = static_cast<const char*>(ckpt.p) + (size_t)k * 2 * n * Bn * rsz;
+                cudaStream_t rst = st;
+                if (nbuf > 1) {
+                    rst = replay_st[bi];
+                    cudaError_t le = cudaStreamWaitEvent(rst, ev_ckpt, 0);
+                    if (le == cudaSuccess && nck - 1 - k >= nbuf) le = cudaStreamWaitEvent(rst, ev_free[bi], 0);
+                    if (le != cudaSuccess) return le;
+                }
                 // the forward runs on the checkpoint's state in place (no copy: with many
                 // adjoints in flight, a copy per chunk queued behind the others' copies);
                 // chunk k's checkpoint is not read again
                 cudaError_t le = launch_fwd_jit(fk, sig, h, t0, t1 - t0, Reducers(), 0ull, 0ull, 1, t1 - t0,
-                                                const_cast<char*>(ck), buf.p, st, ck + (size_t)n * Bn * rsz);
+                                                const_cast<char*>(ck), bp, rst, ck + (size_t)n * Bn * rsz);
                 if (le != cudaSuccess) return le;
+                if (nbuf > 1) {
+                    le = cudaEventRecord(ev_replayed[bi], rst);
+                    if (le == cudaSuccess) le = cudaStreamWaitEvent(st, ev_replayed[bi], 0);
+                    if (le != cudaSuccess) return le;
+                }
                 a.phase = 2;
                 a.k_hi = a.k_lo = k;
                 a.slot_base = t0;
+                a.buf = reinterpret_cast<RT*>(bp);
                 le = cudaLaunchKernel((const void*)jk.fn, grid, dim3(jk.block), args, (size_t)jk.smem, st);
                 if (le != cudaSuccess) return le;
+                if (nbuf > 1) {
+                    le = cudaEventRecord(ev_free[bi], st);
+                    if (le != cudaSuccess) return le;
+                }
             }
+            a.buf = buf0;
             return cudaSuccess;
         }
         const int per = adj_group(n, C, nck);   // checkpoint intervals per launch

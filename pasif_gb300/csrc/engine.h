@@ -112,6 +112,16 @@ struct Batch {
     DevBuf ckpt, buf, pbar, dx0, gfin, gsq, adj_stage, lamc, adj_state;
     DevBuf split;                 // kFP32Ext: values / x0 split into high and low parts (device inputs)
     DevBuf pkbuf;                 // FP32 adjoints: [2P][B] compensated per-chunk gradient totals
+    // Replayed adjoints: streams on which the chunks' forward replays run ahead
+    // of the backward sweep (one per chunk buffer), and their events
+    static constexpr int kReplayBufs = 4;
+    cudaStream_t replay_st[kReplayBufs] = {};
+    cudaEvent_t ev_ckpt = nullptr, ev_replayed[kReplayBufs] = {}, ev_free[kReplayBufs] = {};
+    int replay_prio = 0;
+    Batch() = default;
+    Batch(const Batch&) = delete;
+    Batch& operator=(const Batch&) = delete;
+    ~Batch();
     Literals lit;
     int n_max = 0;
     bool has_sq = false;

@@ -1680,7 +1680,11 @@ int ws_split(int n, bool f32, bool force, bool adjoint, bool ext) {
     // the extended-state mode holds the low parts of the values and the
     // state besides: fewer components per warp (ptxas, 64-state banded system:
     // 4 warps spill 428 bytes forward, 3.9 KB adjoint)
-    const int cpw = force ? 2 : adjoint ? (f32 ? (ext ? 8 : 11) : 6) : (f32 ? (ext ? 12 : 32) : 16);
+    // FP32 adjoints were later cut at 8 components per warp: 64-state banded
+    // system, FP32-Kahan, checkpointed (M adjoint system-steps/s, 6 -> 8
+    // warps): 512 systems 41.6 -> 51.9, 2048 147 -> 177, 4096 250 -> 274;
+    // 10 warps were slower again (37.8 / 118 / 180).
+    const int cpw = force ? 2 : adjoint ? (f32 ? 8 : 6) : (f32 ? (ext ? 12 : 32) : 16);
     int L = std::max(4, (n + cpw - 1) / cpw);
     if (adjoint && f32 && !force) L = std::min(L, 8);
     if (const char* e = std::getenv("PASIF_WS_SLICES")) L = std::atoi(e);   // tuning override

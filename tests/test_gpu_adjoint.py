@@ -237,7 +237,7 @@ def test_adjoint_short_horizons(gpu, N, B, storage):
 @pytest.mark.parametrize("storage", [0, 1 << 30])
 def test_adjoint_banded32_default_slices(gpu, storage):
     """64-state banded system (the 32-DOF serving class), FP32-Kahan: the
-    default warp-sliced adjoint (6 warps) and a 16-warp split give the same
+    default warp-sliced adjoint (8 warps) and a 16-warp split give the same
     bits, replayed from checkpoints (2112 systems: 66 blocks) and stored; the
     gradients are finite and nonzero."""
     w = synth.banded32(n_sys=2112, nsteps=210, sig_len=256)

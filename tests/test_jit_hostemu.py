@@ -333,14 +333,14 @@ def test_generated_warp_sliced_banded32(tmp_path, prec):
 
 def test_generated_adjoint_banded32_default_slices(tmp_path):
     """64-state banded system, FP32-Kahan: the default warp-sliced adjoint
-    (6 warps of 10-11 components) gives the bits of a 16-warp split."""
+    (8 warps of 8 components) gives the bits of a 16-warp split."""
     w = synth.banded32(n_sys=5, nsteps=30, sig_len=64)
     rng = np.random.default_rng(31)
     gf = rng.normal(size=(w.n_sys, w.pattern.n))
     gs = rng.normal(size=w.n_sys)
     sq, N = (0, 5), 30
     rep = Plan(w.pattern, "fp32_kahan").jit_report_adjoint(w.values, sq_mask=(1 << 0) | (1 << 5))
-    assert "slices=6 " in rep.split("// ---- source ----\n", 1)[1].splitlines()[0]
+    assert "slices=8 " in rep.split("// ---- source ----\n", 1)[1].splitlines()[0]
     out = []
     for slicing in (None, True):
         d = os.path.join(str(tmp_path), str(slicing))

@@ -279,3 +279,32 @@ def test_shared_slice_code_same_bits(gpu, monkeypatch, nd, n_sys):
         out[share] = res
     for a, c in zip(out["1"], out["0"]):
         np.testing.assert_array_equal(a, c)
+
+
+@pytest.mark.parametrize("prec", ["fp32_kahan", "fp64"])
+def test_replayed_chunks_ahead_of_the_sweep(gpu, prec):
+    """Checkpointed adjoints of 4200 systems (replayed by the forward kernel,
+    the replays of up to four chunks running ahead of the backward sweep on
+    their own streams): horizons of 2, 3 and 30 chunks and a batch reused
+    across them give the bits of the stored-trajectory adjoint."""
+    rng = np.random.default_rng(808)
+    pat, v = cases.random_system(rng, n=4)
+    B = 4200
+    vals, x0 = cases.random_batch(rng, pat, v, B)
+    x = cases.signals(rng, 2, 200)
+    exc = rng.integers(0, 2, B)
+    gs = rng.normal(size=B)
+    reused = Batch(Plan(pat, prec), vals, x0, exc)
+    reused.adjoint_storage(0)
+    for N in (4, 9, 870):
+        out = []
+        for storage in (0, 1 << 30):
+            b = Batch(Plan(pat, prec), vals, x0, exc)
+            b.adjoint_storage(storage)
+            out.append(b.adjoint(Signals(x, 2, [[0, .5], [1, .5]], prec), 0.02, N, g_sq=gs, sq_comp=(0,),
+                                 sq_start=N // 2))
+        again = reused.adjoint(Signals(x, 2, [[0, .5], [1, .5]], prec), 0.02, N, g_sq=gs, sq_comp=(0,),
+                               sq_start=N // 2)
+        for a, c, d in zip(out[0], out[1], again):
+            np.testing.assert_array_equal(a, c)
+            np.testing.assert_array_equal(a, d)

@@ -320,7 +320,11 @@ int pasif_batch_adjoint_kernel(pasif_batch* b, int* kind);
  * FMA-bound RK4 kernels.  Diagnostic; no reference counterpart. */
 int pasif_fma_peak(int precision, double* flops_per_second);
 
-/* One-shot forward from host buffers: upload, integrate, download. */
+/* One-shot forward from host buffers: upload, integrate, download.  The
+ * device buffers stay with the library for the next call with the same
+ * pattern, precision, forcing window and weights (a repeated call then
+ * allocates and frees nothing), until the process exits; concurrent calls
+ * from other threads use buffers of their own. */
 int pasif_forward(const pasif_pattern* pattern, int precision, int n_sys, const double* values,
                   const double* x0, const int* exc_index, const double* x, int n_exc, int len,
                   int window, const double* im, double h, int step0, int nsteps,

@@ -245,3 +245,27 @@ def test_reserve_requires_inputs_again(gpu):
     fresh.forward(sig, w.h, 300, max_comp=(0,))
     for x, y in zip(b.get(), fresh.get()):
         np.testing.assert_array_equal(x, y)
+
+
+def test_one_shot_forward_reuses_its_buffers(gpu):
+    """pasif_forward keeps its device buffers for the next call with the same
+    pattern, precision and forcing: a sequence of calls that changes the
+    values, the number of systems, the signals, then the pattern, the
+    precision and the window, and comes back, gives the oracle's bits each
+    time."""
+    rng = np.random.default_rng(321)
+    pats = [cases.random_system(rng, n=3), cases.random_system(rng, n=5)]
+    seq = [(0, "fp32_kahan", 2, 70), (0, "fp32_kahan", 2, 70), (0, "fp32_kahan", 2, 130), (1, "fp32_kahan", 2, 50),
+           (1, "fp64", 2, 50), (1, "fp64", 4, 50), (0, "fp32_kahan", 2, 40)]
+    for k, (pi, prec, W, B) in enumerate(seq):
+        pat, v = pats[pi]
+        vals, x0 = cases.random_batch(rng, pat, v, B)
+        x = cases.signals(rng, 3, 60 + 10 * k)
+        exc = rng.integers(0, 3, B)
+        im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W])
+        red = dict(max_comp=[0], max_start=20, sq_comp=[0], sq_start=10)
+        st, mx, sq = forward(pat, vals, x0, exc, x, 0.04, 90, W, im, prec, 0, **red)
+        ost, omx, osq = O.batch_forward(pat, vals, x0, exc, x, 0.04, 90, W, im, prec, 0, **red)
+        np.testing.assert_array_equal(st, ost, err_msg=str(k))
+        np.testing.assert_array_equal(mx, omx, err_msg=str(k))
+        np.testing.assert_array_equal(sq, osq, err_msg=str(k))

@@ -1217,7 +1217,9 @@ void emit_sys_head(std::ostringstream& o, const Pattern& pat, const Emitter& em,
 // terms: +13.5 %), spring chains lose (n = 4, 8, 16: -3 to -19 %: their rows
 // pair with shifted columns, so most packed operands must be assembled), so
 // compensated forwards are packed only for n <= 6 with a destination pair of
-// at least 4 terms on each side.  PASIF_FP32X2 overrides the choice (tuning).
+// at least 4 terms on each side.  The extended-state mode follows the
+// compensated one (2-DOF coupled: packed stages +2 %, packed double-float
+// update +5 % more).  PASIF_FP32X2 overrides the choice (tuning).
 int fwd_paired(const Pattern& pat, const FwdKernelKey& key) {
     if (!key.f32 || key.fast || key.slices >= 2) return 0;
     std::vector<int> cnt(pat.n, 0);
@@ -1231,7 +1233,7 @@ int fwd_paired(const Pattern& pat, const FwdKernelKey& key) {
         dense += cnt[i] >= 4 && cnt[i + 1] >= 4;
     }
     if (both == 0) return 0;
-    int mode = (!key.kahan && !key.ext) ? 2 : (pat.n <= 6 && dense > 0) ? (key.ext ? 1 : 2) : 0;
+    int mode = (!key.kahan && !key.ext) ? 2 : (pat.n <= 6 && dense > 0) ? 2 : 0;
     if (const char* e = std::getenv("PASIF_FP32X2")) mode = std::max(0, std::min(2, std::atoi(e)));
     return mode;
 }

@@ -194,6 +194,31 @@ __device__ __forceinline__ void ext_update(R& hi, R& lo, R sum, R cr, R h, R h6,
     hi = q;
 }
 
+// ext_update on components 2m, 2m+1 at once (packed FP32, the same
+// operations lane by lane).  The product h6 sum is formed by two scalar
+// multiplications: it feeds an add, and ptxas would contract a packed
+// product into a packed add (M2).
+__device__ __forceinline__ void ext_update2(float& hi0, float& hi1, float& lo0, float& lo1, float sum0, float sum1,
+                                            float cr0, float cr1, float h, float h6, float h6lo) {
+    typedef M2 p2;
+    const float2 sum = make_float2(sum0, sum1);
+    const float2 p = make_float2(__fmul_rn(h6, sum0), __fmul_rn(h6, sum1));
+    float2 e = p2::fma(make_float2(h6, h6), sum, make_float2(-p.x, -p.y));
+    e = p2::fma(make_float2(h6lo, h6lo), sum, e);
+    e = p2::fma(make_float2(h, h), make_float2(cr0, cr1), e);
+    const float2 hi = make_float2(hi0, hi1), lo = make_float2(lo0, lo1);
+    const float2 t = p2::add(hi, p);
+    const float2 z = p2::sub(t, hi);
+    const float2 err = p2::add(p2::sub(hi, p2::sub(t, z)), p2::sub(p, z));
+    const float2 l = p2::add(lo, p2::add(err, e));
+    const float2 q = p2::add(t, l);
+    const float2 nl = p2::sub(l, p2::sub(q, t));
+    lo0 = nl.x;
+    lo1 = nl.y;
+    hi0 = q.x;
+    hi1 = q.y;
+}
+
 // (hi, lo) += x (two-sum, renormalised).
 template <typename R>
 __device__ __forceinline__ void ext_add(R& hi, R& lo, R x) {
@@ -365,8 +390,7 @@ __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K
     typedef M<R> m;
     static_assert(!EXT || N > 0, "extended-state steps need a compile-time state size");
     static_assert(!FAST || (!EXT && NSTG == 0), "fast steps are plain forward steps");
-    static_assert(!PAIR || (sizeof(R) == 4 && N > 0 && !FAST && NSTG <= 1 && (!EXT || PAIR == 1)),
-                  "paired steps: FP32 forward; extended state with the scalar update");
+    static_assert(!PAIR || (sizeof(R) == 4 && N > 0 && !FAST && NSTG <= 1), "paired steps: FP32 forward");
     const int n = N ? N : sys.dim();
     if constexpr (PAIR) {
         typedef M2 p2;
@@ -408,9 +432,18 @@ __device__ __forceinline__ void rk4_step(const Sys& sys, V& Q, V& Cm, V& S, V& K
             }
         }
         sys.template rhs<true>(Mi, Mi, uc, K);
-        if constexpr (EXT) {
+        if constexpr (EXT && PAIR == 1) {
 #pragma unroll
             for (int i = 0; i < N; ++i) ext_update(Q[i], Cm[i], m::add(S[i], K[i]), Kc[i], h, h6, h6lo);
+            return;
+        }
+        if constexpr (EXT) {
+#pragma unroll
+            for (int i = 0; i + 1 < N; i += 2) {
+                const float2 sum = p2::add(P(S[i], S[i + 1]), P(K[i], K[i + 1]));
+                ext_update2(Q[i], Q[i + 1], Cm[i], Cm[i + 1], sum.x, sum.y, Kc[i], Kc[i + 1], h, h6, h6lo);
+            }
+            if constexpr (N & 1) ext_update(Q[N - 1], Cm[N - 1], m::add(S[N - 1], K[N - 1]), Kc[N - 1], h, h6, h6lo);
             return;
         }
         if constexpr (KAHAN && PAIR == 1) {
@@ -657,7 +690,7 @@ __device__ __forceinline__ void fwd_core_iv(const Sys& sys, const FwdArgs<R>& a,
     constexpr int W = WP::W;
     constexpr bool FASTK = WP::FAST && HTRAJ == 0 && !EXT;   // fast steps: plain forwards only
     // paired (f32x2) steps: FP32 forwards (extended state: packed stages only)
-    constexpr int PAIRK = (WP::PAIR && !FASTK) ? (EXT ? 1 : WP::PAIR) : 0;
+    constexpr int PAIRK = (WP::PAIR && !FASTK) ? WP::PAIR : 0;
     constexpr unsigned SPI = W == 0 ? 1u : (unsigned)(W / 2);
     constexpr int STG = HTRAJ == 2 ? adj_slot_vecs<R>() : 0;
     const long long B = a.B;

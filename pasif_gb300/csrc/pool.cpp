@@ -107,6 +107,18 @@ int Pool::create(const Pattern& pat, int precision, int window, const double* im
     PL_CUDA(cudaMemset(p->remain_.p, 0, C * sizeof(int)), "cudaMemset");
     PL_CUDA(cudaMemset(p->vals_.p, 0, P * C * rs), "cudaMemset");
     PL_CUDA(cudaMemset(p->state_.p, 0, (size_t)n * C * rs), "cudaMemset");
+    // every per-slot field defined from the start (a free slot's are read by
+    // no kernel, but nothing is left uninitialised)
+    PL_CUDA(cudaMemset(p->comp_.p, 0, (size_t)n * C * rs), "cudaMemset");
+    PL_CUDA(cudaMemset(p->mx_.p, 0, (size_t)n * C * rs), "cudaMemset");
+    PL_CUDA(cudaMemset(p->sq_.p, 0, C * rs), "cudaMemset");
+    PL_CUDA(cudaMemset(p->sqc_.p, 0, C * rs), "cudaMemset");
+    PL_CUDA(cudaMemset(p->step_.p, 0, C * sizeof(unsigned)), "cudaMemset");
+    PL_CUDA(cudaMemset(p->ebase_.p, 0, C * sizeof(long long)), "cudaMemset");
+    PL_CUDA(cudaMemset(p->lim_.p, 0, C * sizeof(long long)), "cudaMemset");
+    PL_CUDA(cudaMemset(p->len_.p, 0, C * sizeof(unsigned)), "cudaMemset");
+    PL_CUDA(cudaMemset(p->mstart_.p, 0, C * sizeof(int)), "cudaMemset");
+    PL_CUDA(cudaMemset(p->sstart_.p, 0, C * sizeof(int)), "cudaMemset");
     // highest priority: a chunk's blocks are scheduled ahead of queued blocks of
     // lower-priority work (e.g. adjoint sweeps), which bounds forward latency
     int prio_least = 0, prio_greatest = 0;

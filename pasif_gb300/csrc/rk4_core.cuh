@@ -1579,12 +1579,15 @@ __device__ __forceinline__ void ws_pool(SL& sl, const PoolArgs<R>& p, R* sm, int
     a.traj_every = 1;
     a.traj_slots = 0;
     a.step0 = 0;
+    // A slot without steps in this chunk (free, finished, or a lane past the
+    // pool) still runs the block's step loop for the exchanges and barriers,
+    // but reads no forcing: its signal fields may be stale or never written.
     Forcing<R> frc = p.frc;
-    frc.len = p.len[b];
-    frc.total = p.lim[b];
+    frc.len = mine ? p.len[b] : 0u;
+    frc.total = mine ? p.lim[b] : 0;
     RunCtx rc;
-    rc.ebase = p.ebase[b];
-    rc.step0 = p.step[b];
+    rc.ebase = mine ? p.ebase[b] : 0;
+    rc.step0 = mine ? p.step[b] : 0u;
     rc.nsteps = mine;
     rc.max_start = p.max_start[b];
     rc.sq_start = p.sq_start[b];

@@ -22,6 +22,17 @@ from . import serving as S
 from . import synth
 
 
+def adjoint_workers_for(n: int) -> int:
+    """Adjoint workers of a served class with n states (see run)."""
+    if n >= 100:
+        return 6
+    if n >= 60:
+        return 10
+    if n >= 16:
+        return 4
+    return 3 if n >= 8 else 2
+
+
 def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, capacity=16384,
         arena_samples=1 << 25, adjoint_budget=96 << 30, adjoint_workers=None, adjoint_storage=3 << 30, check=6,
         log=None) -> dict:
@@ -31,8 +42,13 @@ def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, cap
     t = time.perf_counter()
     reqs = [(sr.arrival, S.make_request(sr, specs[sr.dof])) for sr in stream]
     t_gen = time.perf_counter() - t
-    if adjoint_workers is None:   # more workers where one adjoint is long and uses few SMs
-        adjoint_workers = {d: 6 if s.pattern.n >= 60 else 4 if s.pattern.n >= 24 else 2 for d, s in specs.items()}
+    if adjoint_workers is None:
+        # More workers where one adjoint is long and holds few SMs, most for the
+        # class whose warp-sliced adjoint cannot share code (the banded 32-DOF
+        # system, one block per SM).  Measured on GB300, this stream: 2-6
+        # workers per class p99 4.1-5.0 s; these counts 3.65-3.9 s (p50
+        # 150-370 ms); more still (3-12) p99 3.4-3.7 s but forward p99 2.8 s.
+        adjoint_workers = {d: adjoint_workers_for(s.pattern.n) for d, s in specs.items()}
     srv = S.Server(specs, precision, capacity, arena_samples, adjoint_budget, adjoint_workers,
                    reserve=(4096, 200_000, 4 * 200_003), adjoint_storage=adjoint_storage)
     t = time.perf_counter()

@@ -493,11 +493,24 @@ struct Slicing {
     int sq_owner = 0;
 };
 
+// Whether the first half of the states are displacements whose derivative is
+// the matching velocity alone (x_i' = x_{n/2+i}, the first-order form of a
+// mechanical system).
+bool velocity_form(int n, const std::vector<std::vector<Term>>& dt) {
+    if (n < 4 || (n & 1)) return false;
+    for (int i = 0; i < n / 2; ++i)
+        if (dt[i].size() != 1 || dt[i][0].kind != 0 || dt[i][0].ops[0] != n / 2 + i) return false;
+    return true;
+}
+
 // Components ordered by reverse Cuthill-McKee on the interaction graph, cut
 // into L contiguous runs of about equal work, so that strongly coupled
 // components share a warp and few values cross warps.
+// dof_pairs (patterns in velocity form): the pairs (x_i, x_{n/2+i}) in DOF
+// order, cut into L runs of equal size, so that the interior slices of a
+// banded or chained system are translates of one another.
 Slicing make_slicing(const Pattern& pat, const std::vector<std::vector<Term>>& dt, int L, unsigned long long sq_mask,
-                     bool adjoint) {
+                     bool adjoint, bool dof_pairs = false) {
     const int n = pat.n;
     std::vector<std::vector<int>> adj(n);
     std::vector<double> wt(n, 4.0);
@@ -531,14 +544,23 @@ Slicing make_slicing(const Pattern& pat, const std::vector<std::vector<Term>>& d
         }
     }
     std::reverse(order.begin(), order.end());
+    const bool by_dof = dof_pairs && velocity_form(n, dt);
+    if (by_dof) {
+        order.clear();
+        for (int i = 0; i < n / 2; ++i) {
+            order.push_back(i);
+            order.push_back(n / 2 + i);
+        }
+    }
     double total = 0.0;
     for (double w : wt) total += w;
     Slicing s;
     s.owner.assign(n, 0);
     std::vector<std::vector<int>> runs(L);
     double cum = 0.0;
-    for (int v : order) {
-        int k = (int)((cum + 0.5 * wt[v]) * L / total);
+    for (size_t r = 0; r < order.size(); ++r) {
+        const int v = order[r];
+        int k = by_dof ? (int)(r / 2 * L / (order.size() / 2)) : (int)((cum + 0.5 * wt[v]) * L / total);
         k = std::max(0, std::min(L - 1, k));
         runs[k].push_back(v);
         cum += wt[v];
@@ -716,17 +738,64 @@ std::vector<SliceGroup> share_slices(const std::vector<std::string>& src, std::o
     return groups;
 }
 
+std::string ws_source_impl(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, int mode, int roll_force,
+                           int* distinct, int dof_force = -1);
+
+// Text that identifies a pattern's structure (memo keys).
+std::string pattern_key(const Pattern& pat) {
+    std::ostringstream k;
+    k << pat.n << ':';
+    for (const std::vector<int>* v : {&pat.k_ptr, &pat.k_col, &pat.g_idx, &pat.l_idx, &pat.p_idx, &pat.f_idx}) {
+        for (int x : *v) k << x << ',';
+        k << ';';
+    }
+    return k.str();
+}
+
+// Cut by displacement/velocity pairs (make_slicing's dof_pairs) where the
+// default cut into L warps gives mostly distinct slices and this one gives at
+// most L/2 distinct structs: a banded 32-DOF system (64 states) cut into 8
+// warps has 8 distinct slices in the default order, 3 by pairs (the two ends
+// and one shared interior struct).  Decided on the FP32 source with values
+// loaded at run time, memoised per pattern.
+bool ws_by_dof(const Pattern& pat, const std::vector<std::vector<Term>>& dt, int L, bool adjoint) {
+    if (L < 4 || !velocity_form(pat.n, dt) || std::getenv("PASIF_WS_RCM")) return false;
+    static std::mutex mu;
+    static std::map<std::string, bool> memo;
+    const std::string mk = pattern_key(pat) + (adjoint ? "a" : "f") + std::to_string(L);
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = memo.find(mk);
+        if (it != memo.end()) return it->second;
+    }
+    FwdKernelKey key;
+    key.f32 = true;
+    key.kahan = true;
+    key.slices = L;
+    int d0 = 0, d1 = 0;
+    ws_source_impl(pat, Literals(), key, adjoint ? 2 : 0, 0, &d0, 0);
+    bool dof = false;
+    if (2 * d0 > L) {
+        ws_source_impl(pat, Literals(), key, adjoint ? 2 : 0, 0, &d1, 1);
+        dof = 2 * d1 <= L;
+    }
+    std::lock_guard<std::mutex> g(mu);
+    memo[mk] = dof;
+    return dof;
+}
+
 // Source of the warp-sliced forward (mode 0: pk_fwd over FwdArgs), serving-
 // pool (mode 1: pk_pool over PoolArgs) or exact-adjoint (mode 2: pk_adj over
 // AdjArgs) kernel.
 // roll_force: -1 = the rule below, 0 / 1 = unrolled / rolled stages.
 // *distinct: number of distinct slice structs after share_slices.
 std::string ws_source_impl(const Pattern& pat, const Literals& lit, const FwdKernelKey& key, int mode, int roll_force,
-                           int* distinct) {
+                           int* distinct, int dof_force) {
     const int n = pat.n;
     const bool adj = mode == 2;
     const auto dt = dest_terms(pat);
-    const Slicing sl = make_slicing(pat, dt, key.slices, adj ? 0ull : key.sq_mask, adj);
+    const bool by_dof = dof_force >= 0 ? dof_force == 1 : ws_by_dof(pat, dt, key.slices, adj);
+    const Slicing sl = make_slicing(pat, dt, key.slices, adj ? 0ull : key.sq_mask, adj, by_dof);
     auto S = [](long long v) { return std::to_string(v); };
     // every term in the global order of the VJP scatter (GenSys::vjp): K rows, Gamma, Lambda, Psi, forcing
     std::vector<std::pair<int, Term>> scatter;   // (destination, term)
@@ -1606,8 +1675,11 @@ namespace {
 // 4.0e9 -> 5.5e9; adjoint 64-DOF chain 8 -> 16 warps 3.6e8 -> 4.5e8 adjoint
 // system-steps/s, 32-DOF chain 6 -> 16 warps 4.7e8 -> 1.0e9, 16-DOF chain 4
 // -> 8 warps 1.45e9 -> 1.89e9.  So: 8 states per warp forward, 4 adjoint, at
-// most 16 warps, where that cut shares.  Patterns whose slices differ (the
-// banded system with random cubic entries) keep the register-bound split.
+// most 16 warps, where that cut shares (in the default order or by
+// displacement/velocity pairs, ws_by_dof: 64-state banded system, 2048
+// systems, forward 4 -> 8 warps 2.08e9 -> 2.77e9, adjoint 8 -> 16 warps
+// 1.84e8 -> 2.73e8).  Patterns whose slices differ in both cuts keep the
+// register-bound split.
 int ws_more_if_shared(const Pattern& pat, int L, bool allowed, bool adjoint) {
     if (!allowed || std::getenv("PASIF_WS_SLICES") || std::getenv(adjoint ? "PASIF_WS_SLICES_ADJ" : "PASIF_WS_SLICES_FWD"))
         return L;
@@ -1616,20 +1688,7 @@ int ws_more_if_shared(const Pattern& pat, int L, bool allowed, bool adjoint) {
     // memoised per pattern: the check generates the kernel source
     static std::mutex mu;
     static std::map<std::string, bool> memo;
-    std::ostringstream k;
-    k << pat.n << (adjoint ? 'a' : 'f') << L2 << ':';
-    for (int v : pat.k_ptr) k << v << ',';
-    k << ';';
-    for (int v : pat.k_col) k << v << ',';
-    k << ';';
-    for (int v : pat.g_idx) k << v << ',';
-    k << ';';
-    for (int v : pat.l_idx) k << v << ',';
-    k << ';';
-    for (int v : pat.p_idx) k << v << ',';
-    k << ';';
-    for (int v : pat.f_idx) k << v << ',';
-    const std::string key = k.str();
+    const std::string key = pattern_key(pat) + (adjoint ? "a" : "f") + std::to_string(L2);
     {
         std::lock_guard<std::mutex> g(mu);
         auto it = memo.find(key);

@@ -320,9 +320,16 @@ def test_generated_pool_matches_oracle(tmp_path, monkeypatch, prec, seed, W, sli
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan", "fp32_ext"])
 def test_generated_warp_sliced_banded32(tmp_path, prec):
-    """64-state banded system: the default kernel is warp-sliced (8 warps,
-    components crossing warps through shared memory); equals the oracle."""
+    """64-state banded system: the default kernel is warp-sliced (components
+    crossing warps through shared memory); FP32-Kahan cuts it by
+    displacement/velocity pairs into 8 warps whose interior slices share one
+    struct.  Equals the oracle."""
     w = synth.banded32(n_sys=6, nsteps=150, sig_len=256)
+    if prec == "fp32_kahan":
+        src = Plan(w.pattern, prec).jit_report(w.values, window=w.window, im=w.im)
+        src = src.split("// ---- source ----\n", 1)[1]
+        assert "slices=8 " in src.splitlines()[0]
+        assert _distinct_structs(src) <= 4
     got = run_emulated(tmp_path, w.pattern, w.values, w.x0, w.exc_index, w.signals, w.window, w.im, w.h, 0,
                        w.nsteps, prec, slicing=None if prec != "fp64" else True)
     ref, _, _ = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,
@@ -333,16 +340,19 @@ def test_generated_warp_sliced_banded32(tmp_path, prec):
 
 def test_generated_adjoint_banded32_default_slices(tmp_path):
     """64-state banded system, FP32-Kahan: the default warp-sliced adjoint
-    (8 warps of 8 components) gives the bits of a 16-warp split."""
+    (16 warps of 2 displacement/velocity pairs, at most 8 distinct slice
+    structs) gives the bits of the thread-per-system adjoint."""
     w = synth.banded32(n_sys=5, nsteps=30, sig_len=64)
     rng = np.random.default_rng(31)
     gf = rng.normal(size=(w.n_sys, w.pattern.n))
     gs = rng.normal(size=w.n_sys)
     sq, N = (0, 5), 30
     rep = Plan(w.pattern, "fp32_kahan").jit_report_adjoint(w.values, sq_mask=(1 << 0) | (1 << 5))
-    assert "slices=8 " in rep.split("// ---- source ----\n", 1)[1].splitlines()[0]
+    rep = rep.split("// ---- source ----\n", 1)[1]
+    assert "slices=16 " in rep.splitlines()[0]
+    assert 2 * _distinct_structs(rep) <= 16
     out = []
-    for slicing in (None, True):
+    for slicing in (None, False):
         d = os.path.join(str(tmp_path), str(slicing))
         os.makedirs(d)
         out.append(run_emulated_adjoint(d, w.pattern, "fp32_kahan", slicing, w.values, w.x0, w.exc_index, w.signals,

@@ -1680,10 +1680,20 @@ namespace {
 // systems, forward 4 -> 8 warps 2.08e9 -> 2.77e9, adjoint 8 -> 16 warps
 // 1.84e8 -> 2.73e8).  Patterns whose slices differ in both cuts keep the
 // register-bound split.
-int ws_more_if_shared(const Pattern& pat, int L, bool allowed, bool adjoint) {
-    if (!allowed || std::getenv("PASIF_WS_SLICES") || std::getenv(adjoint ? "PASIF_WS_SLICES_ADJ" : "PASIF_WS_SLICES_FWD"))
+// The extended-state and FP64 forwards gain from finer shared cuts too
+// (4096 systems unless noted, system-steps/s, default -> 8 -> 16 warps):
+// FP32-EXT 64-state chain 1.27e9 -> 4.69e9 -> 4.66e9, 64-state banded (2048
+// systems) 8.4e8 -> 1.79e9 -> 1.97e9, 128-state chain 1.50e9 -> 2.40e9 ->
+// 3.07e9, but 32-state chain 6.1e9 -> 5.9e9 -> 6.0e9; FP64 32-state chain
+// 4.9e8 -> 5.2e8 -> 5.5e8, 64-state chain 2.73e8 -> 2.77e8 -> 2.81e8,
+// 64-state banded 7.8e7 -> 7.9e7 -> 8.3e7, 128-state chain 1.35e8 ->
+// 1.35e8 -> 1.41e8.  So: FP32-EXT 4 states per warp from 64 states, FP64 16
+// warps from 32 states.
+// L2: the finer cut to take where it shares (0: none).
+int ws_more_if_shared(const Pattern& pat, int L, int L2, bool adjoint) {
+    if (L2 <= 0 || std::getenv("PASIF_WS_SLICES") || std::getenv(adjoint ? "PASIF_WS_SLICES_ADJ" : "PASIF_WS_SLICES_FWD"))
         return L;
-    const int L2 = std::min(16, pat.n / (adjoint ? 4 : 8));
+    L2 = std::min(L2, pat.n);
     if (L2 <= L) return L;
     // memoised per pattern: the check generates the kernel source
     static std::mutex mu;
@@ -1713,7 +1723,8 @@ int ws_slices(const Pattern& pat, bool f32, bool force, int B, bool ext) {
         const bool small_batch = B > 0 && B <= 8192;
         if (f32 ? n < 28 : (n < 3 || (n < 8 && !small_batch))) return 0;
     }
-    return ws_more_if_shared(pat, ws_split(n, f32, force, false, ext), f32 && !force && !ext, false);
+    const int L2 = force ? 0 : !f32 ? (n >= 32 ? 16 : 0) : ext ? (n >= 64 ? std::min(16, n / 4) : 0) : std::min(16, n / 8);
+    return ws_more_if_shared(pat, ws_split(n, f32, force, false, ext), L2, false);
 }
 
 int ws_slices_adjoint(const Pattern& pat, bool f32, bool force, bool ext) {
@@ -1723,7 +1734,8 @@ int ws_slices_adjoint(const Pattern& pat, bool f32, bool force, bool ext) {
     // states 0.75, 8 states 0.62, 4 states 0.93, 2 states 1.12; FP64 2 states
     // 0.68, 4-8 states 0.33-0.44.
     if (n < 2 || n > kWsMaxN || (!force && f32 && n < 5)) return 0;
-    return ws_more_if_shared(pat, ws_split(n, f32, force, true, ext), f32 && !force && !ext, true);
+    return ws_more_if_shared(pat, ws_split(n, f32, force, true, ext), f32 && !force && !ext ? std::min(16, n / 4) : 0,
+                             true);
 }
 
 int ws_split(int n, bool f32, bool force, bool adjoint, bool ext) {

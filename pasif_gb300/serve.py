@@ -24,10 +24,8 @@ from . import synth
 
 def adjoint_workers_for(n: int) -> int:
     """Adjoint workers of a served class with n states (see run)."""
-    if n >= 100:
-        return 6
     if n >= 60:
-        return 10
+        return 6
     if n >= 16:
         return 4
     return 3 if n >= 8 else 2
@@ -43,11 +41,12 @@ def run(rate=200.0, duration=1.5, seed=5, precision="fp32_kahan", dofs=None, cap
     reqs = [(sr.arrival, S.make_request(sr, specs[sr.dof])) for sr in stream]
     t_gen = time.perf_counter() - t
     if adjoint_workers is None:
-        # More workers where one adjoint is long and holds few SMs, most for the
-        # class whose warp-sliced adjoint cannot share code (the banded 32-DOF
-        # system, one block per SM).  Measured on GB300, this stream: 2-6
-        # workers per class p99 4.1-5.0 s; these counts 3.65-3.9 s (p50
-        # 150-370 ms); more still (3-12) p99 3.4-3.7 s but forward p99 2.8 s.
+        # More workers where one adjoint is long and holds few SMs (the 32- and
+        # 64-DOF classes, one block per SM).  Measured on GB300, this stream,
+        # p99 over runs: 2/2/3/4/4/10/6 workers (1..64 DOF) 2.3-2.8 s; these
+        # counts (2/2/3/4/4/6/6) 2.22-2.25 s, forward p99 1.1 s; 6 for the
+        # 8-DOF class or 8 for the 64-DOF class changed nothing beyond the
+        # run-to-run spread (2.05-2.75 s).
         adjoint_workers = {d: adjoint_workers_for(s.pattern.n) for d, s in specs.items()}
     srv = S.Server(specs, precision, capacity, arena_samples, adjoint_budget, adjoint_workers,
                    reserve=(4096, 200_000, 4 * 200_003), adjoint_storage=adjoint_storage)

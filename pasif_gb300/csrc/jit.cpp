@@ -1734,8 +1734,12 @@ int ws_slices_adjoint(const Pattern& pat, bool f32, bool force, bool ext) {
     // states 0.75, 8 states 0.62, 4 states 0.93, 2 states 1.12; FP64 2 states
     // 0.68, 4-8 states 0.33-0.44.
     if (n < 2 || n > kWsMaxN || (!force && f32 && n < 5)) return 0;
-    return ws_more_if_shared(pat, ws_split(n, f32, force, true, ext), f32 && !force && !ext ? std::min(16, n / 4) : 0,
-                             true);
+    // FP64, shared slices: 2 states per warp up to 32 states (GB300, 4096
+    // systems, default -> 8 -> 16 warps, adjoint system-steps/s: 16-state
+    // chain 3.30e8 -> 3.63e8 -> 3.59e8, 32-state chain 1.79e8 -> 1.83e8 ->
+    // 1.87e8; 64-state chain 9.1e7 -> 9.1e7 -> 9.0e7 keeps its cut).
+    const int L2 = force ? 0 : f32 ? (ext ? 0 : std::min(16, n / 4)) : (n <= 32 ? std::min(16, n / 2) : 0);
+    return ws_more_if_shared(pat, ws_split(n, f32, force, true, ext), L2, true);
 }
 
 int ws_split(int n, bool f32, bool force, bool adjoint, bool ext) {

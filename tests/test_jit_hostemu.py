@@ -455,3 +455,55 @@ def test_generated_adjoint_chain16_sliced_equals_thread(tmp_path, prec):
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
     assert np.abs(out[0][0]).max() > 0
+
+
+def _scattered_velocity_form(seed, nd=32):
+    """x_i' = v_i; v_i' = linear in x_i, v_i and two random x_j; one cubic
+    term per DOF on random components: first-order mechanical form whose
+    couplings follow no band."""
+    from pasif_gb300.system import Pattern
+    rng = np.random.default_rng(seed)
+    n = 2 * nd
+    rows, cols, vals = [], [], []
+    for i in range(nd):
+        rows.append(i); cols.append(nd + i); vals.append(1.0)
+    for i in range(nd):
+        for j, v in ((i, -2.0), (nd + i, -0.05)):
+            rows.append(nd + i); cols.append(j); vals.append(v)
+        for j in rng.choice(nd, size=2, replace=False):
+            if j != i:
+                rows.append(nd + i); cols.append(int(j)); vals.append(0.1)
+    lam = [(nd + i, int(rng.integers(nd)), int(rng.integers(nd)), int(rng.integers(nd))) for i in range(nd)]
+    pat, order = Pattern.from_dense_lists(n, rows, cols, [], lam, [], [nd])
+    v = np.concatenate([np.asarray(vals)[order], rng.normal(0, 0.1, len(lam)), [1.0]])
+    return pat, np.repeat(v[None, :], 2, axis=0)
+
+
+def test_pair_cut_only_where_it_shares(monkeypatch):
+    """Velocity-form patterns are cut by displacement/velocity pairs only when
+    that gives shared slice code: the banded 32-DOF system takes it (8
+    forward warps, at most 4 structs; in the default order its 8 slices all
+    differ), a system with scattered couplings keeps the default cut (its
+    source is the same with the pair cut switched off)."""
+    w = synth.banded32(n_sys=4, nsteps=10, sig_len=256)
+    src = Plan(w.pattern, "fp32_kahan").jit_report(w.values, window=w.window, im=w.im)
+    src = src.split("// ---- source ----\n", 1)[1]
+    assert "slices=8 " in src.splitlines()[0]
+    assert _distinct_structs(src) <= 4
+    monkeypatch.setenv("PASIF_WS_SLICES_FWD", "8")
+    monkeypatch.setenv("PASIF_WS_RCM", "1")
+    rcm = Plan(w.pattern, "fp32_kahan").jit_report(w.values, window=w.window, im=w.im)
+    assert _distinct_structs(rcm.split("// ---- source ----\n", 1)[1]) == 8
+    monkeypatch.delenv("PASIF_WS_SLICES_FWD")
+    monkeypatch.delenv("PASIF_WS_RCM")
+    pat, vals = _scattered_velocity_form(7)
+    out = []
+    for rcm_only in (False, True):
+        if rcm_only:
+            monkeypatch.setenv("PASIF_WS_RCM", "1")
+        for prec in ("fp32_kahan", "fp64"):
+            rep = Plan(pat, prec).jit_report(vals)
+            out.append(rep.split("// ---- source ----\n", 1)[1])
+            rep = Plan(pat, prec).jit_report_adjoint(vals, sq_mask=1)
+            out.append(rep.split("// ---- source ----\n", 1)[1])
+    assert out[:4] == out[4:]

@@ -366,19 +366,18 @@ def _distinct_structs(src):
     return len(re.findall(r"^struct SL\d+ \{", src, flags=re.M))
 
 
-@pytest.mark.parametrize("prec", ["fp32_kahan", "fp64"])
+@pytest.mark.parametrize("prec", ["fp32_kahan", "fp64", "fp32_ext"])
 def test_shared_slices_chain_forward(tmp_path, prec):
     """32-DOF spring chain (64 states), default warp-sliced kernels: the
     interior slices are translates of one another and share one struct
-    (runtime bases, per-warp value table); FP32 cuts the chain into 8 warps.
-    Equal to the oracle."""
+    (runtime bases, per-warp value table); FP32-Kahan cuts the chain into 8
+    warps, FP64 and the extended-state mode into 16.  Equal to the oracle."""
     w = synth.chain8(n_sys=5, nsteps=120, nd=32)
     src = Plan(w.pattern, prec).jit_report(w.values, window=w.window, im=w.im)
     src = src.split("// ---- source ----\n", 1)[1]
     L = int(re.search(r"slices=(\d+)", src).group(1))
-    if prec == "fp32_kahan":
-        assert L == 8
-        assert 2 * _distinct_structs(src) <= L, (_distinct_structs(src), L)
+    assert L == (8 if prec == "fp32_kahan" else 16)
+    assert 2 * _distinct_structs(src) <= L, (_distinct_structs(src), L)
     got = run_emulated(tmp_path, w.pattern, w.values, w.x0, w.exc_index, w.signals, w.window, w.im, w.h, 0,
                        w.nsteps, prec)
     ref, _, _ = O.batch_forward(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, w.nsteps, w.window, w.im,

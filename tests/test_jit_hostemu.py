@@ -419,6 +419,28 @@ def test_shared_slices_chain_adjoint(tmp_path):
     np.testing.assert_array_equal(dx, odx)
 
 
+def test_default_fp64_adjoint_chain8_shared(tmp_path):
+    """8-DOF spring chain (16 states, the config-3 system), FP64: the default
+    adjoint is cut into 8 warps of 2 states, some of them sharing code (the
+    slices holding the summed components differ), and gives the oracle's
+    exact adjoint bit for bit."""
+    w = synth.chain8(n_sys=4, nsteps=40, nd=8)
+    rng = np.random.default_rng(43)
+    gf = rng.normal(size=(w.n_sys, w.pattern.n))
+    gs = rng.normal(size=w.n_sys)
+    sq, N = (0, 3), 40
+    rep = Plan(w.pattern, "fp64").jit_report_adjoint(w.values, sq_mask=(1 << 0) | (1 << 3))
+    rep = rep.split("// ---- source ----\n", 1)[1]
+    assert "slices=8 " in rep.splitlines()[0]
+    assert _distinct_structs(rep) < 8
+    dv, dx = run_emulated_adjoint(str(tmp_path), w.pattern, "fp64", None, w.values, w.x0, w.exc_index, w.signals,
+                                  np.asarray(w.im), gf, gs, N, sq, N // 3, h=w.h)
+    odv, odx = O.batch_adjoint(w.pattern, w.values, w.x0, w.exc_index, w.signals, w.h, N, w.window, w.im, gf, gs, sq,
+                               N // 3)
+    np.testing.assert_array_equal(dv, odv)
+    np.testing.assert_array_equal(dx, odx)
+
+
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan", "fp32_ext"])
 @pytest.mark.parametrize("slicing", [False, True])
 @pytest.mark.parametrize("split", [1, 2])

@@ -268,18 +268,40 @@ def test_generated_pool_matches_oracle(tmp_path, monkeypatch, prec, seed, W, sli
         monkeypatch.setenv("PASIF_FP32X2", "2")
     rng = np.random.default_rng(900 + seed)
     pat, v = cases.random_system(rng)
+    if slicing and pat.n < 2:
+        pytest.skip("one component: nothing to slice")
+    src = _check_pool(tmp_path, rng, pat, v, prec, W, slicing)
+    if packed and pat.n >= 2:
+        assert "packed FP32" in src.splitlines()[0]
+
+
+def test_generated_pool_banded32_pair_cut(tmp_path):
+    """Serving-pool chunk kernel of the 64-state banded system (the served
+    32-DOF class), FP32-Kahan, default layout: warp-sliced, cut by
+    displacement/velocity pairs into 8 warps with shared slice code; every
+    job equals the oracle run of that job alone, bit for bit."""
+    if shutil.which("g++") is None:
+        pytest.skip("no host C++ compiler")
+    rng = np.random.default_rng(950)
+    w = synth.banded32(n_sys=1, nsteps=10, sig_len=64)
+    src = _check_pool(tmp_path, rng, w.pattern, w.values[0], "fp32_kahan", 2, None)
+    assert "slices=8 " in src.splitlines()[0]
+    assert 2 * _distinct_structs(src) <= 8
+
+
+def _check_pool(tmp_path, rng, pat, v, prec, W, slicing):
+    """Run random jobs of pattern `pat` (values around v) through the host-
+    emulated pool kernel and compare every job with the oracle; returns the
+    kernel source."""
     C, chunk = 7, 16
     jobs = _pool_jobs(rng, pat, v, C, W)
     im = np.stack([np.arange(W) / W, 1 - np.arange(W) / W]) if W else None
     max_comp = (0,)
     sq_comp = (0,) if pat.n == 1 else (0, pat.n - 1)
-    if slicing and pat.n < 2:
-        pytest.skip("one component: nothing to slice")
     src = Plan(pat, prec, slicing=slicing).jit_report_pool(W, im, max_comp, sq_comp)
     src = src.split("// ---- source ----\n", 1)[1]
-    assert ("warp-sliced" in src) == slicing
-    if packed and pat.n >= 2:
-        assert "packed FP32" in src.splitlines()[0]
+    if slicing is not None:
+        assert ("warp-sliced" in src) == slicing
     d = str(tmp_path)
     exe, env = build_emulator(d, src, "EMU_POOL")
     dt = np.float64 if prec == "fp64" else np.float32
@@ -316,6 +338,7 @@ def test_generated_pool_matches_oracle(tmp_path, monkeypatch, prec, seed, W, sli
         np.testing.assert_array_equal(mx[k:k + m, list(max_comp)], omx)
         np.testing.assert_array_equal(sq[k:k + m], osq)
         k += m
+    return src
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32_kahan", "fp32_ext"])
